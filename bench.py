@@ -1,0 +1,320 @@
+"""Benchmark of the explicit time loop (damian.par run_explicit) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload NAME] [--form fp64|fp32] [--scale S]
+
+A bench step is one time step of the whole batch of right-hand sides on the
+workload's mesh.  Metric: element-steps x RHS per second (N_e * R * steps / s),
+inputs resident in HBM, timed with CUDA events on the library's own stream.
+Multi-GPU runs are independent replicas (the path shards but is not built
+multi-GPU): weak scaling, value = sum over ranks.
+
+--impl reference times the CPU oracle (the C++ restatement of the reference's
+per-element loop; the Fortran/MPI reference cannot be built here) with every
+host thread, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+for p in (HERE, os.path.join(HERE, "damian.par_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+FORMS = {"fp64": 0, "fp32": 1}
+DEFAULT_WORKLOAD = ("canyon", "fp64")
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        return ws, rank, local, dist, torch
+    return 1, 0, local, None, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce_max(dist, torch, x):
+    if dist is None:
+        return x
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        mine = [r for r in rows if r[0] == str(self.gpu)] or rows
+        if not mine:
+            return None
+        sm = [float(r[1]) for r in mine if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in mine if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in mine for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(mine)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def kernel_bytes(name, m, R, fp64):
+    """Algorithmic bytes one launch of `name` must move (what the roofline uses).
+
+    ne, nn: elements, nodes; ndof = 2 nn; s = state word (8 FP64, 4 FP32).
+      k_elem_ref/k_elem64   read u, u- (2*ndof*s*R), element data (conn 16 +
+                            (mu,lambda) 16 + mass 8 + damping slot 4), write
+                            the element forces 8*s*R per element
+      k_node_ref/k_node64   read the element forces once (8*s*R per element),
+                            the gather lists (4 B per incidence), m_full 16 per
+                            node, write u+ (ndof*s*R)
+      k_drm*                read corner coordinates (64 B), write 16 forces*s*R
+                            per DRM element
+      k_hang*               hanging nodes 3 values in/1 out, receivers
+      k_step32              FP32 increment form, fused: read u_hi, Kahan term
+                            and increment, write all three (6*ndof*4*R), read
+                            element data (conn 16 + coef 16) and lists
+    """
+    ne, nn, ns = m.nelems, m.nnodes, m.problem.nseismic
+    nh, nr = m.problem.nhanging, m.problem.nrecv
+    ndof = 2 * nn
+    s = 8 if fp64 else 4
+    inc = 4 * ne
+    if name in ("k_elem_ref", "k_elem64"):
+        return 2 * ndof * s * R + ne * 44 + ne * 8 * s * R
+    if name in ("k_node_ref", "k_node64"):
+        return ne * 8 * s * R + 4 * inc + 16 * nn + ndof * s * R
+    if name.startswith("k_drm"):
+        return ns * (64 + 16 * s * R)
+    if name.startswith("k_hang"):
+        return nh * 2 * 3 * s * R + nr * (4 * 2 * s * R + 2 * 8 * R)
+    if name.startswith("k_step32"):
+        return 6 * ndof * 4 * R + ne * 32 + 4 * inc
+    return None
+
+
+def ncu_traffic(kernel, workload):
+    """Per-launch DRAM bytes from the committed ncu summary, if one exists."""
+    try:
+        with open(os.path.join(HERE, "profiles", "ncu_traffic.json")) as f:
+            d = json.load(f)
+        v = d.get(workload, {}).get(kernel)
+        return v.get("bytes_per_launch") if isinstance(v, dict) else v
+    except Exception:
+        return None
+
+
+def input_bytes(m):
+    p, L = m.problem, int(m.eptr()[-1]) - 1
+    return (4 * (m.nelems + 1) + 4 * L + L + 16 * m.nnodes + 4 * m.nelems + 40 * p.nmat + 4 * m.nnodes
+            + 12 * p.nhanging + 8 * p.nseismic + 40 * p.nrhs + 20 * p.nrecv)
+
+
+def cpu_baseline(m, target_s=12.0, rhs=0):
+    """Oracle on all host threads over a bounded sample (steps chosen for ~target_s)."""
+    from oracle import oracle
+    nt = os.cpu_count() or 1
+    probe = oracle.run(m, rhs=rhs, nsteps=2, nthreads=nt, want_u=False)["seconds"]
+    per_step = max(probe / 2.0, 1e-6)
+    steps = int(max(1, min(m.problem.nsteps, target_s / per_step)))
+    r = oracle.run(m, rhs=rhs, nsteps=steps, nthreads=nt, want_u=False)
+    val = m.nelems * steps / r["seconds"]
+    return {"value": val, "unit": "elem-steps*rhs/s", "cores": nt, "kind": "port",
+            "sample": "oracle per-element FP64 loop, rhs %d, %d of %d steps, %d elements, %d threads"
+                      % (rhs, steps, m.problem.nsteps, m.nelems, nt)}
+
+
+def run_reference(args, ws, rank, dist):
+    if rank != 0:
+        return
+    from exfem import workloads
+    m = workloads.build(args.workload, scale=args.scale, steps=20000)
+    from oracle import oracle
+    nt = os.cpu_count() or 1
+    probe = oracle.run(m, nsteps=2, nthreads=nt, want_u=False)["seconds"] / 2.0
+    budget = 150.0 / max(args.steps + args.warmup, 1)      # whole run within a few minutes
+    sample = int(max(1, min(m.problem.nsteps, budget / max(probe, 1e-6))))
+    secs = []
+    for i in range(args.warmup + args.steps):
+        r = oracle.run(m, nsteps=sample, nthreads=nt, want_u=False)
+        if i >= args.warmup:
+            secs.append(r["seconds"])
+    t = float(np.mean(secs))
+    val = m.nelems * sample / t
+    out = {"metric": "elem-steps/s", "value": val, "unit": "elem-steps*rhs/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1000.0 * t / sample, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": args.workload, "scale": args.scale, "elements": m.nelems, "rhs_timed": 1,
+                      "sample_steps": sample},
+           "impl": "reference",
+           "cpu_baseline": {"value": val, "unit": "elem-steps*rhs/s", "cores": nt, "kind": "port",
+                            "sample": "%d time steps of rhs 0 per bench step" % sample},
+           "e2e": {"value": val, "unit": "elem-steps*rhs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args, ws, rank, local, dist, torch):
+    from exfem import workloads
+    from exfem.abi import ExfemError
+    from exfem.gpu import Solver
+
+    form = FORMS[args.form]
+    fp64 = form == 0
+    total = args.warmup + args.steps
+    m = workloads.build(args.workload, scale=args.scale, steps=max(total, 8))
+    R = m.problem.nrhs
+    s = Solver(m, precision=form, device=local)
+    s.init_explicit()
+    s.run(args.warmup)
+    s.sync()
+    barrier(dist)
+    clk = ClockSampler(local).start() if rank == 0 else None
+    l0 = s.launches
+    ms = C.c_double(0)
+    rc = s.lib.exfem_gpu_run_timed(s.h, int(args.steps), C.byref(ms))
+    if rc != 0:
+        raise ExfemError(rc, s.lib.exfem_gpu_last_error(s.h).decode())
+    s.sync()
+    launches = s.launches - l0
+    clocks = clk.stop() if clk else None
+    barrier(dist)
+    t_ms = allreduce_max(dist, torch, ms.value)
+    s.close()
+    value = ws * m.nelems * R * args.steps / (t_ms / 1000.0)
+
+    # per-kernel CUDA-event times on a fresh context (no graph, same stream)
+    prof_steps = max(4, min(64, args.steps))
+    mp = workloads.build(args.workload, scale=args.scale, steps=prof_steps + 2)
+    sp = Solver(mp, precision=form, device=local)
+    sp.init_explicit()
+    sp.run(2)
+    ms_arr = (C.c_double * 16)()
+    nm_arr = (C.c_char_p * 16)()
+    nk = sp.lib.exfem_gpu_profile_kernels(sp.h, prof_steps, ms_arr, nm_arr, 16)
+    kern = {nm_arr[i].decode(): ms_arr[i] for i in range(max(nk, 0))}
+    sp.close()
+    dom = max(kern, key=lambda k: kern[k]) if kern else None
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if dom:
+        b = kernel_bytes(dom, m, R, fp64)
+        achieved = b / (kern[dom] / 1000.0) / 1e9 if b else None
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "peak_kind": peak_kind,
+                "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                "traffic": ncu_traffic(dom, args.workload), "algorithmic_bytes": b,
+                "kernel_ms": kern[dom], "kernels_ms": kern}
+
+    # end to end through the C ABI with host buffers: create (uploads) + init +
+    # run + seismogram read-back
+    e2e_steps = args.steps
+    me = workloads.build(args.workload, scale=args.scale, steps=e2e_steps)
+    t0 = time.perf_counter()
+    se = Solver(me, precision=form, device=local)
+    se.init_explicit()
+    se.run(e2e_steps)
+    seis = se.seismograms()
+    se.close()
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": ws * me.nelems * R * e2e_steps / t_e2e, "unit": "elem-steps*rhs/s",
+           "h2d_bytes_per_step": input_bytes(me), "d2h_bytes_per_step": int(seis.nbytes),
+           "note": "one request per bench step: create + init_explicit + %d steps + seismograms" % e2e_steps}
+
+    if rank != 0:
+        return
+    cpu = cpu_baseline(m) if ws == 1 else None
+    out = {"metric": "elem-steps/s", "value": value, "unit": "elem-steps*rhs/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64" if fp64 else "f32+kahan", "data": "synthetic (seeded deck)",
+           "config": {"workload": args.workload, "form": args.form, "scale": args.scale, "elements": m.nelems,
+                      "nodes": m.nnodes, "rhs": R, "hanging": m.problem.nhanging,
+                      "l2": "no flush: a bench step is one time step; the state of this workload is %.1f MB"
+                            % ((2 * m.nnodes * R * (8 if fp64 else 4) * (2 if fp64 else 4)) / 1e6),
+                      "parallelism": "replicas" if ws > 1 else "single"},
+           "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD[0])
+    ap.add_argument("--form", default=DEFAULT_WORKLOAD[1], choices=sorted(FORMS))
+    ap.add_argument("--scale", type=float, default=1.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local, dist, torch = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, dist)
+    else:
+        run_ours(args, ws, rank, local, dist, torch)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,109 @@
+// exfem_ctx.h — device context shared by the FP64 and FP32 kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "exfem_gpu.h"
+#include "exfem_plan.h"
+
+namespace exfem {
+
+// Plane-wave constants as the kernels read them (pwaves.f90 module state).
+struct DevWave {
+    int kind;
+    double alpha, beta, fp;
+    double sine, cose, sinf, cosf;
+    double amp0, wa1, wb1;
+    double wui[6];
+    double t0;
+};
+
+// Device arrays common to both arithmetic forms.
+struct DevModel {
+    int nn, ne, R, n_active, n_hang, ns, nrecv, nsave, io;
+    double dt, a1, a2, a3;
+    double worigin_x, worigin_y;
+    const int *econn;        // 4 per element
+    const double *ecoef;     // 4 per element (FP64)
+    const float *ecoef32;    // 4 per element (FP32)
+    const double *emulam;    // 2 per element: (mu, lambda)
+    const double *emass;     // per element
+    const int *edamp;        // per element, -1 or slot
+    const double *edampv;    // 8 per slot
+    const double *nxy;       // 2 per node (internal)
+    const int *tptr, *tlist; // gather lists (active nodes)
+    const int *dptr, *dlist; // DRM gather lists (active nodes)
+    const double *inv_mfull; // 2 per active node
+    const double *mfull;     // 2 per active node (m_full, divided by)
+    const int *hang;         // 3 per hanging entry
+    const int *s_elem, *s_kind;
+    const int *rnode;        // 4 per receiver (corners; hanging ones read as anchor averages)
+    const double *rw;        // 4 per receiver (shape-function weights)
+    const int *rsoil;
+    const double *rxy;       // 2 per receiver
+    const DevWave *waves;    // R
+    const int *ownptr, *ownlist;   // own element incidences, all nodes, element order
+    const int *odptr, *odlist;     // own DRM incidences, all nodes, seismic order
+    const int *lptr, *llist;       // anchor links (h, other anchor), m_hanging order
+    // FP32 increment form
+    const float *ncoefA;           // per active node: (a1 M - a2 Cx, a1 M - a2 Cy) pairs
+    const float *nD;               // per node: D = a1 M + a2 C (x, y)
+    const float *inv_mfull32;      // 2 per active node
+    // mutable state
+    double *fdrm;            // ns * 16 * R DRM forces (stiffness part, mass part)
+    double *seis;            // R * nsave * nrecv * 2
+    int *d_step;             // steps completed (device counter)
+    unsigned *d_blocks;      // last-block counter
+    int *d_flag;             // watchdog flags
+};
+
+struct Ctx {
+    Plan plan;
+    exfem_opts opts;
+    int device = 0;
+    int precision = EXFEM_FP64;
+    cudaStream_t stream = nullptr;
+    DevModel dm{};
+    std::vector<void *> allocs;
+    size_t bytes = 0;
+    // FP64 state: u[2] ping-pong + element forces
+    double *u64[2] = {nullptr, nullptr};
+    double *ef64 = nullptr;
+    // FP32 state: hi[2] ping-pong, compensation, increment
+    float *uhi[2] = {nullptr, nullptr};
+    float *ucomp = nullptr;
+    float *udel[2] = {nullptr, nullptr};
+    int parity = 0;          // index of the current u buffer
+    int steps_done = 0;
+    bool inited = false;
+    long long launches = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    int graph_parity = -1;
+    int block_threads = 128;
+    int rhs_per_thread = 1;
+    std::string err;
+    // per-launch event marks while exfem_gpu_profile_kernels runs
+    bool prof_on = false;
+    std::vector<std::pair<const char *, cudaEvent_t>> marks;
+};
+
+// Records a profiling mark after a launch (no-op unless profiling).
+void mark(Ctx &c, const char *kernel);
+
+// Launchers of the reference-order FP64 file.
+int f64ref_launch_drm_elem_node(Ctx &c, int par);
+int f64_launch_hang(Ctx &c, double *unew, int mode);
+
+// Launchers implemented by the FP32 file.
+int f32_alloc(Ctx &c);
+int f32_init(Ctx &c);
+int f32_launch_step(Ctx &c, int par);
+int f32_launch_sample0(Ctx &c, int par);
+int f32_get_u(Ctx &c, int rhs, std::vector<double> &out_internal);
+
+}  // namespace exfem

@@ -1,0 +1,156 @@
+// exfem_device.cuh — device functions shared by the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "exfem_ctx.h"
+
+namespace exfem {
+
+// Q4 square plane-strain stiffness applied to one element's corner
+// displacements, K(mu, lambda) u with K = calck(mu, lambda)
+// (formulation.f90:276-313).  The bilinear field is split into its modes
+// c1 = d/dxi, c2 = d/deta, c3 = xi*eta per component; the fully integrated
+// energy of the square element is
+//   2(l+2m)(c1x^2 + c2y^2) + 4 l c1x c2y + 2 m (c2x + c1y)^2 + (2/3)(l+3m)(c3x^2 + c3y^2)
+// (modes scaled by 1/4), whose gradient gives the eight nodal forces with
+// about 34 operations instead of the 64 multiply-adds of the dense 8x8 product.
+// k = ((l+2m)/4, l/4, m/4, (l+3m)/12); corners in CSR order TL, TR, BR, BL.
+template <typename T>
+__host__ __device__ __forceinline__ void q4_ku(T A, T B, T C, T D, const T ux[4], const T uy[4], T fx[4], T fy[4]) {
+    T px = ux[2] - ux[0], qx = ux[1] - ux[3];
+    T c1x = px + qx, c2x = px - qx, c3x = (ux[0] + ux[2]) - (ux[1] + ux[3]);
+    T py = uy[2] - uy[0], qy = uy[1] - uy[3];
+    T c1y = py + qy, c2y = py - qy, c3y = (uy[0] + uy[2]) - (uy[1] + uy[3]);
+    T F1 = A * c1x + B * c2y;
+    T F2 = A * c2y + B * c1x;
+    T S = C * (c2x + c1y);
+    T Gx = D * c3x, Gy = D * c3y;
+    T ax = F1 + S, bx = F1 - S;
+    fx[0] = Gx - ax; fx[1] = bx - Gx; fx[2] = ax + Gx; fx[3] = -(bx + Gx);
+    T ay = S + F2, by = S - F2;
+    fy[0] = Gy - ay; fy[1] = by - Gy; fy[2] = ay + Gy; fy[3] = -(by + Gy);
+}
+
+// Force of corner `c` only (the node-centric gather needs one corner).
+template <typename T>
+__host__ __device__ __forceinline__ void q4_ku_corner(T A, T B, T C, T D, const T ux[4], const T uy[4], int c, T &fx, T &fy) {
+    T px = ux[2] - ux[0], qx = ux[1] - ux[3];
+    T c1x = px + qx, c2x = px - qx, c3x = (ux[0] + ux[2]) - (ux[1] + ux[3]);
+    T py = uy[2] - uy[0], qy = uy[1] - uy[3];
+    T c1y = py + qy, c2y = py - qy, c3y = (uy[0] + uy[2]) - (uy[1] + uy[3]);
+    T F1 = A * c1x + B * c2y;
+    T F2 = A * c2y + B * c1x;
+    T S = C * (c2x + c1y);
+    T Gx = D * c3x, Gy = D * c3y;
+    // corner sign pattern of (P, Q, G): TL(-,-,+) TR(+,-,-) BR(+,+,+) BL(-,+,-)
+    T sP = (c == 1 || c == 2) ? T(1) : T(-1);
+    T sQ = (c >= 2) ? T(1) : T(-1);
+    T sG = (c == 0 || c == 2) ? T(1) : T(-1);
+    fx = sP * F1 + sQ * S + sG * Gx;
+    fy = sP * S + sQ * F2 + sG * Gy;
+}
+
+// Consistent mass (calcsqm/9, formulation.f90:256-268) times v for one
+// component: weights 4 (self), 2 (edge neighbours), 1 (opposite corner).
+__host__ __device__ __forceinline__ void q4_msq(const double v[4], double out[4]) {
+    for (int k = 0; k < 4; ++k)
+        out[k] = (4.0 * v[k] + 2.0 * v[(k + 1) & 3] + v[(k + 2) & 3] + 2.0 * v[(k + 3) & 3]) / 9.0;
+}
+
+// One Ricker term with its first two time derivatives (pwaves.f90:157-169).
+__host__ __device__ __forceinline__ void ricker3(double fp, double d, double out[3]) {
+    double q = fp * d;
+    double v2 = q * q;
+    double e = exp(v2);
+    out[0] = (1.0 - 2.0 * v2) / e;
+    out[1] = (2.0 * v2 - 3.0) * (fp * fp) * d / e;
+    out[2] = -2.0 * (4.0 * (v2 * v2) - 12.0 * v2 + 3.0) * (fp * fp) / e;
+}
+
+// planewave (pwaves.f90:100-217): u[comp][col], comp x/z, col u/du/ddu.
+// `ncol` limits the work to the first columns needed (1: displacement only).
+__host__ __device__ __forceinline__ void planewave(const DevWave &w, double t, double x1, double x3, double ux[3],
+                                          double uz[3]) {
+    double v0;
+    if (w.kind == EXFEM_WAVE_P) v0 = (x1 * w.sine - x3 * w.cose) / w.alpha;
+    else v0 = (x1 * w.sinf - x3 * w.cosf) / w.beta;
+    double v1 = (x1 * w.sine + x3 * w.cose) / w.alpha;
+    double v2 = (x1 * w.sinf + x3 * w.cosf) / w.beta;
+    double r0[3], r1[3], r2[3];
+    ricker3(w.fp, t - v0, r0);
+    ricker3(w.fp, t - v1, r1);
+    ricker3(w.fp, t - v2, r2);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double ipx = r0[c] * w.wui[0] * w.amp0, ipz = r0[c] * w.wui[1] * w.amp0;
+        double rpx = r1[c] * w.wui[2] * w.wa1, rpz = r1[c] * w.wui[3] * w.wa1;
+        double rsx = r2[c] * w.wui[4] * w.wb1, rsz = r2[c] * w.wui[5] * w.wb1;
+        ux[c] = ipx + rpx + rsx;
+        uz[c] = ipz + rpz + rsz;
+    }
+}
+
+// Displacement column only.
+__host__ __device__ __forceinline__ void planewave_u(const DevWave &w, double t, double x1, double x3, double &ux,
+                                            double &uz) {
+    double v0;
+    if (w.kind == EXFEM_WAVE_P) v0 = (x1 * w.sine - x3 * w.cose) / w.alpha;
+    else v0 = (x1 * w.sinf - x3 * w.cosf) / w.beta;
+    double v1 = (x1 * w.sine + x3 * w.cose) / w.alpha;
+    double v2 = (x1 * w.sinf + x3 * w.cosf) / w.beta;
+    double q0 = w.fp * (t - v0), q1 = w.fp * (t - v1), q2 = w.fp * (t - v2);
+    double s0 = q0 * q0, s1 = q1 * q1, s2 = q2 * q2;
+    double r0 = (1.0 - 2.0 * s0) / exp(s0), r1 = (1.0 - 2.0 * s1) / exp(s1), r2 = (1.0 - 2.0 * s2) / exp(s2);
+    ux = r0 * w.wui[0] * w.amp0 + r1 * w.wui[2] * w.wa1 + r2 * w.wui[4] * w.wb1;
+    uz = r0 * w.wui[1] * w.amp0 + r1 * w.wui[3] * w.wa1 + r2 * w.wui[5] * w.wb1;
+}
+
+// DRM exterior masks of wave_reactions (model.f90:778-793), bit k = dof k.
+__host__ __device__ __forceinline__ unsigned drm_mask(int kind) {
+    switch (kind) {
+        case 2: return 0xC3u;   // SE_SVERL: T T F F F F T T
+        case 4: return 0x3Cu;   // SE_SVERR: F F T T T T F F
+        case 1: return 0xF0u;   // SE_SHORI: F F F F T T T T
+        case 6: return 0xF3u;   // SE_CORNL: T T F F T T T T
+        case 5: return 0xFCu;   // SE_CORNR: F F T T T T T T
+        default: return 0u;
+    }
+}
+
+// Effective DRM forces of one boundary element (wave_reactions,
+// model.f90:745-800, with multdrm formulation.f90:378-393 for K and for the
+// consistent mass): p = -K_be u0_e on boundary dofs, +K_eb u0_b on exterior
+// dofs, plus the same with M_cons*mass on the free-field acceleration.
+__host__ __device__ __forceinline__ void drm_forces(const double k[4], double mass, unsigned e, const double u0[8],
+                                           const double a0[8], double p[8]) {
+    double uex[4], uey[4], ubx[4], uby[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        bool ex = (e >> (2 * c)) & 1u, ey = (e >> (2 * c + 1)) & 1u;
+        uex[c] = ex ? u0[2 * c] : 0.0;       ubx[c] = ex ? 0.0 : u0[2 * c];
+        uey[c] = ey ? u0[2 * c + 1] : 0.0;   uby[c] = ey ? 0.0 : u0[2 * c + 1];
+    }
+    double kex[4], key[4], kbx[4], kby[4];
+    q4_ku<double>(k[0], k[1], k[2], k[3], uex, uey, kex, key);
+    q4_ku<double>(k[0], k[1], k[2], k[3], ubx, uby, kbx, kby);
+    double aex[4], aey[4], abx[4], aby[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        bool ex = (e >> (2 * c)) & 1u, ey = (e >> (2 * c + 1)) & 1u;
+        aex[c] = ex ? a0[2 * c] : 0.0;       abx[c] = ex ? 0.0 : a0[2 * c];
+        aey[c] = ey ? a0[2 * c + 1] : 0.0;   aby[c] = ey ? 0.0 : a0[2 * c + 1];
+    }
+    double mex[4], mey[4], mbx[4], mby[4];
+    q4_msq(aex, mex); q4_msq(aey, mey); q4_msq(abx, mbx); q4_msq(aby, mby);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        bool ex = (e >> (2 * c)) & 1u, ey = (e >> (2 * c + 1)) & 1u;
+        double pkx = ex ? kbx[c] : -kex[c], pky = ey ? kby[c] : -key[c];
+        double pmx = ex ? mbx[c] : -mex[c], pmy = ey ? mby[c] : -mey[c];
+        p[2 * c] = pkx + pmx * mass;
+        p[2 * c + 1] = pky + pmy * mass;
+    }
+}
+
+}  // namespace exfem

@@ -1,0 +1,284 @@
+// exfem_f64ref_nofma.cu — FP64 step kernels in the reference's operation order.
+//
+// This translation unit is compiled with -fmad=false: every product and sum
+// rounds separately, as the reference's Fortran (and the CPU oracle) does, so
+// the per-element terms, the per-dof sums and the update reproduce
+// run_explicit (explicit.f90:125-153) operation for operation:
+//   * localr = (a3 u - a1 u-)*m; localr += a2*c*u-; then the
+//     dgemv('N',8,8,-1,K,8,u,1,1,localr,1) of explicit.f90:139-140 column by
+//     column with K = calck(mu, lambda) (formulation.f90:276-313);
+//   * each dof sums its DRM terms (seismic order, K part then mass part,
+//     model.f90:794-798) and then its element terms in element order;
+//   * anchors add half of each hanging node's sum in m_hanging order
+//     (sum_reactanchors, halving form), then u = r / m_full (explicit.f90:148).
+// The only differences left are the exp() of the free field (CUDA vs the host
+// libm, ulp level).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "exfem_ctx.h"
+#include "exfem_device.cuh"
+
+namespace exfem {
+
+namespace {
+
+// calck (formulation.f90:276-313), column-major k[col*8+row].
+__device__ __forceinline__ void calck(double m, double l, double k[64]) {
+    const double v[64] = {
+        (3.0 * m + l) / 3.0, (m + l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, -(m - l) / 4.0,
+        -(3.0 * m + l) / 6.0, -(m + l) / 4.0, l / 6.0, (m - l) / 4.0,
+        (m + l) / 4.0, (3.0 * m + l) / 3.0, (m - l) / 4.0, l / 6.0,
+        -(m + l) / 4.0, -(3.0 * m + l) / 6.0, -(m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0,
+        -(3.0 * m + 2.0 * l) / 6.0, (m - l) / 4.0, (3.0 * m + l) / 3.0, -(m + l) / 4.0,
+        l / 6.0, -(m - l) / 4.0, -(3.0 * m + l) / 6.0, (m + l) / 4.0,
+        -(m - l) / 4.0, l / 6.0, -(m + l) / 4.0, (3.0 * m + l) / 3.0,
+        (m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, (m + l) / 4.0, -(3.0 * m + l) / 6.0,
+        -(3.0 * m + l) / 6.0, -(m + l) / 4.0, l / 6.0, (m - l) / 4.0,
+        (3.0 * m + l) / 3.0, (m + l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, -(m - l) / 4.0,
+        -(m + l) / 4.0, -(3.0 * m + l) / 6.0, -(m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0,
+        (m + l) / 4.0, (3.0 * m + l) / 3.0, (m - l) / 4.0, l / 6.0,
+        l / 6.0, -(m - l) / 4.0, -(3.0 * m + l) / 6.0, (m + l) / 4.0,
+        -(3.0 * m + 2.0 * l) / 6.0, (m - l) / 4.0, (3.0 * m + l) / 3.0, -(m + l) / 4.0,
+        (m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, (m + l) / 4.0, -(3.0 * m + l) / 6.0,
+        -(m - l) / 4.0, l / 6.0, -(m + l) / 4.0, (3.0 * m + l) / 3.0};
+#pragma unroll
+    for (int i = 0; i < 64; ++i) k[i] = v[i];
+}
+
+// calcsqm (formulation.f90:256-268) entry (i, j): same component only,
+// 4 on the diagonal, 2 for edge-adjacent corners, 1 for the opposite corner.
+__device__ __forceinline__ double sqm(int i, int j) {
+    if ((i & 1) != (j & 1)) return 0.0;
+    int d = ((j >> 1) - (i >> 1)) & 3;
+    double v = (d == 0) ? 4.0 : (d == 2 ? 1.0 : 2.0);
+    return v / 9.0;
+}
+
+// One thread per (boundary element, rhs): wave_reactions with the dense
+// multdrm loops (formulation.f90:378-393).  Stores the stiffness part and
+// the mass part separately (each is added to the reactions on its own).
+__global__ void k_drm_ref(DevModel m) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.ns * m.R) return;
+    int s = (int)(t / m.R), r = (int)(t % m.R);
+    int step = *(volatile int *)m.d_step + 1;
+    const DevWave w = m.waves[r];
+    double outt = (double)step * m.dt - w.t0;
+    int ie = m.s_elem[s];
+    double u0[8], a0[8];
+    for (int k = 0; k < 4; ++k) {
+        int x = m.econn[4 * ie + k];
+        double ox = m.nxy[2 * x] - m.worigin_x, oz = m.nxy[2 * x + 1] - m.worigin_y;
+        double ux[3], uz[3];
+        planewave(w, outt, ox, oz, ux, uz);
+        u0[2 * k] = ux[0]; u0[2 * k + 1] = uz[0];
+        a0[2 * k] = ux[2]; a0[2 * k + 1] = uz[2];
+    }
+    unsigned e = drm_mask(m.s_kind[s]);
+    double K[64];
+    calck(m.emulam[2 * ie], m.emulam[2 * ie + 1], K);
+    double pk[8], pm[8];
+    for (int i = 0; i < 8; ++i) { pk[i] = 0.0; pm[i] = 0.0; }
+    for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 8; ++j)
+            if (((e >> j) & 1u) && !((e >> i) & 1u)) {
+                pk[i] = pk[i] - K[j * 8 + i] * u0[j];
+                pk[j] = pk[j] + K[i * 8 + j] * u0[i];
+                pm[i] = pm[i] - sqm(i, j) * a0[j];
+                pm[j] = pm[j] + sqm(j, i) * a0[i];
+            }
+    double mass = m.emass[ie];
+    for (int k = 0; k < 8; ++k) {
+        m.fdrm[((size_t)s * 16 + k) * m.R + r] = pk[k];
+        m.fdrm[((size_t)s * 16 + 8 + k) * m.R + r] = pm[k] * mass;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_elem_ref(DevModel m, const double *__restrict__ u,
+                                                  const double *__restrict__ um, double *__restrict__ ef) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.ne * m.R) return;
+    int e = (int)(t / m.R), r = (int)(t % m.R);
+    const int4 c = reinterpret_cast<const int4 *>(m.econn)[e];
+    const int cn[4] = {c.x, c.y, c.z, c.w};
+    double lu[8], lp[8];
+    const size_t R = m.R;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        size_t ix = ((size_t)cn[k] * 2) * R + r;
+        lu[2 * k] = u[ix]; lu[2 * k + 1] = u[ix + R];
+        lp[2 * k] = um[ix]; lp[2 * k + 1] = um[ix + R];
+    }
+    double mass = m.emass[e];
+    double lr[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) lr[k] = (m.a3 * lu[k] - m.a1 * lp[k]) * mass;
+    int ds = m.edamp[e];
+    if (ds >= 0) {
+        const double *dv = m.edampv + (size_t)ds * 8;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) lr[k] = lr[k] + m.a2 * dv[k] * lp[k];
+    }
+    double2 ml = reinterpret_cast<const double2 *>(m.emulam)[e];
+    double K[64];
+    calck(ml.x, ml.y, K);
+#pragma unroll
+    for (int col = 0; col < 8; ++col) {
+        double temp = -1.0 * lu[col];
+#pragma unroll
+        for (int row = 0; row < 8; ++row) lr[row] = lr[row] + temp * K[col * 8 + row];
+    }
+    if (R == 1) {
+        double4 *o = reinterpret_cast<double4 *>(ef + (size_t)e * 8);
+        o[0] = make_double4(lr[0], lr[1], lr[2], lr[3]);
+        o[1] = make_double4(lr[4], lr[5], lr[6], lr[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) ef[((size_t)e * 8 + k) * R + r] = lr[k];
+    }
+}
+
+// Sum of one node's own terms in the reference order.
+__device__ __forceinline__ void own_sum(const DevModel &m, int n, int r, const double *__restrict__ ef, double &rx,
+                                        double &ry) {
+    const size_t R = m.R;
+    rx = 0.0;
+    ry = 0.0;
+    for (int q = m.odptr[n]; q < m.odptr[n + 1]; ++q) {
+        int sc = m.odlist[q];
+        size_t b = ((size_t)(sc >> 2) * 16 + 2 * (sc & 3)) * R + r;
+        rx = rx + m.fdrm[b];
+        ry = ry + m.fdrm[b + R];
+        rx = rx + m.fdrm[b + 8 * R];
+        ry = ry + m.fdrm[b + 9 * R];
+    }
+    for (int q = m.ownptr[n]; q < m.ownptr[n + 1]; ++q) {
+        int ec = __ldg(m.ownlist + q);
+        size_t b = ((size_t)(ec >> 2) * 8 + 2 * (ec & 3)) * R + r;
+        rx = rx + ef[b];
+        ry = ry + ef[b + R];
+    }
+}
+
+__global__ void __launch_bounds__(128) k_node_ref(DevModel m, const double *__restrict__ ef, double *__restrict__ unew) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.n_active * m.R) return;
+    int n = (int)(t / m.R), r = (int)(t % m.R);
+    double rx, ry;
+    own_sum(m, n, r, ef, rx, ry);
+    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
+        double hx, hy;
+        own_sum(m, m.llist[2 * q], r, ef, hx, hy);
+        rx = rx + hx / 2.0;
+        ry = ry + hy / 2.0;
+    }
+    const size_t R = m.R;
+    unew[((size_t)n * 2) * R + r] = rx / m.mfull[2 * n];
+    unew[((size_t)n * 2 + 1) * R + r] = ry / m.mfull[2 * n + 1];
+}
+
+__device__ __forceinline__ void load_u64(const DevModel &m, const double *u, int node, int r, double &vx, double &vy) {
+    const size_t R = m.R;
+    if (node < m.n_active) {
+        vx = u[((size_t)node * 2) * R + r];
+        vy = u[((size_t)node * 2 + 1) * R + r];
+    } else {   // hanging corner: set_dispshanging value (u_a + u_b)/2
+        int i = node - m.n_active;
+        int a = m.hang[3 * i + 1], b = m.hang[3 * i + 2];
+        vx = (u[((size_t)a * 2) * R + r] + u[((size_t)b * 2) * R + r]) / 2.0;
+        vy = (u[((size_t)a * 2 + 1) * R + r] + u[((size_t)b * 2 + 1) * R + r]) / 2.0;
+    }
+}
+
+// Hanging nodes (set_dispshanging) and receiver samples (visu_field,
+// visualization.f90:156-181): blocks [0, nb_hang) do the hanging nodes, the
+// rest sample the receivers on save steps.  mode 1 records the step-0 sample.
+__global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict__ unew, int nb_hang, int mode) {
+    int step = (mode == 1) ? 0 : *(volatile int *)m.d_step + 1;
+    const size_t R = m.R;
+    if ((int)blockIdx.x < nb_hang) {
+        long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (mode == 0 && t < (long long)m.n_hang * m.R) {
+            int i = (int)(t / m.R), r = (int)(t % m.R);
+            int h = m.hang[3 * i], a = m.hang[3 * i + 1], b = m.hang[3 * i + 2];
+            for (int d = 0; d < 2; ++d)
+                unew[((size_t)h * 2 + d) * R + r] = (unew[((size_t)a * 2 + d) * R + r] + unew[((size_t)b * 2 + d) * R + r]) / 2.0;
+        }
+    } else if (step % m.io == 0) {
+        long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
+        if (t < (long long)m.nrecv * m.R) {
+            int i = (int)(t % m.nrecv), r = (int)(t / m.nrecv);
+            int slot = step / m.io;
+            double fx = 0.0, fy = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                double vx, vy;
+                load_u64(m, unew, m.rnode[4 * i + k], r, vx, vy);
+                double w = m.rw[4 * i + k];
+                fx = fx + w * vx;
+                fy = fy + w * vy;
+            }
+            if (m.rsoil[i]) {
+                const DevWave wv = m.waves[r];
+                double time = m.dt * (double)slot * (double)m.io;
+                double dx, dz;
+                planewave_u(wv, time - wv.t0, m.rxy[2 * i] - m.worigin_x, m.rxy[2 * i + 1] - m.worigin_y, dx, dz);
+                fx = fx + dx;
+                fy = fy + dz;
+            }
+            size_t o = (((size_t)r * m.nsave + slot) * m.nrecv + i) * 2;
+            m.seis[o] = fx;
+            m.seis[o + 1] = fy;
+            if (!isfinite(fx) || !isfinite(fy)) atomicOr(m.d_flag, 1);
+        }
+    }
+    if (mode == 0) {   // last block advances the device step counter
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            unsigned prev = atomicAdd(m.d_blocks, 1u);
+            if (prev == gridDim.x - 1) {
+                *m.d_step = *m.d_step + 1;
+                *m.d_blocks = 0u;
+                __threadfence();
+            }
+        }
+    }
+}
+
+inline int nblocks(long long work, int threads) { return (int)std::max<long long>(1, (work + threads - 1) / threads); }
+
+}  // namespace
+
+int f64ref_launch_drm_elem_node(Ctx &c, int par) {
+    DevModel &m = c.dm;
+    double *u = c.u64[par], *um = c.u64[par ^ 1];
+    const int T = 128;
+    if (m.ns > 0) {
+        k_drm_ref<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+        c.launches++;
+        mark(c, "k_drm_ref");
+    }
+    k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, u, um, c.ef64);
+    mark(c, "k_elem_ref");
+    k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, c.ef64, um);
+    mark(c, "k_node_ref");
+    c.launches += 2;
+    return cudaGetLastError() == cudaSuccess ? EXFEM_OK : EXFEM_E_CUDA;
+}
+
+// Hanging + receivers for both FP64 variants; mode 1 = step-0 sample.
+int f64_launch_hang(Ctx &c, double *unew, int mode) {
+    DevModel &m = c.dm;
+    const int T = 128;
+    int nbh = mode == 1 ? 0 : (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);
+    int nbr = (int)(((long long)m.nrecv * m.R + T - 1) / T);
+    if (nbh + nbr == 0) return EXFEM_OK;
+    k_hang_ref<<<nbh + nbr, T, 0, c.stream>>>(m, unew, nbh, mode);
+    c.launches++;
+    mark(c, "k_hang_ref");
+    return cudaGetLastError() == cudaSuccess ? EXFEM_OK : EXFEM_E_CUDA;
+}
+
+}  // namespace exfem

@@ -1,0 +1,642 @@
+// exfem_gpu.cu — C ABI (include/exfem_gpu.h) and the FP64 step kernels.
+//
+// One time step of run_explicit (explicit.f90:125-153) is four kernels:
+//   k_drm       DRM effective forces of the boundary layer at t = (i)*dt
+//               (additive_reactions -> wave_reactions, model.f90:745-800)
+//   k_elem64    per-element localr = (a3 u - a1 u-)*m + a2 c*u- - K u
+//               (explicit.f90:130-140) into an element-force buffer
+//   k_node64    per non-hanging node: gather its element and DRM terms (terms
+//               of a hanging node it anchors at weight 1/2: sum_reactanchors
+//               in halving form), u+ = r / m_full (explicit.f90:143-148);
+//               the gather replaces the element scatter and the MPI sums, so
+//               no atomics are needed
+//   k_hang      u_h = (u_a + u_b)/2 (set_dispshanging, model.f90:612-624) and
+//               the in-loop receiver samples (visu_field) on save steps
+// The step counter lives on the device so a captured CUDA graph of several
+// steps can be replayed unchanged.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "exfem_ctx.h"
+#include "exfem_device.cuh"
+#include "exfem_gpu.h"
+#include "exfem_plan.h"
+
+using namespace exfem;
+
+namespace {
+
+thread_local std::string g_create_err;
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            c.err = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+            return EXFEM_E_CUDA;                                                              \
+        }                                                                                     \
+    } while (0)
+
+__device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
+
+// ---------------------------------------------------------------- DRM ----
+// One thread per (boundary element, rhs).  Free field at the element's four
+// corners, then multdrm for K and for the consistent mass (model.f90:766-798).
+__global__ void k_drm(DevModel m) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.ns * m.R) return;
+    int s = (int)(t / m.R), r = (int)(t % m.R);
+    int step = read_step(m) + 1;
+    const DevWave w = m.waves[r];
+    double outt = (double)step * m.dt - w.t0;   // timetransform(m_wttoorigin, i*dt)
+    int ie = m.s_elem[s];
+    double u0[8], a0[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int x = m.econn[4 * ie + k];
+        double ox = m.nxy[2 * x] - m.worigin_x, oz = m.nxy[2 * x + 1] - m.worigin_y;
+        double ux[3], uz[3];
+        planewave(w, outt, ox, oz, ux, uz);
+        u0[2 * k] = ux[0]; u0[2 * k + 1] = uz[0];
+        a0[2 * k] = ux[2]; a0[2 * k + 1] = uz[2];
+    }
+    double kc[4] = {m.ecoef[4 * ie], m.ecoef[4 * ie + 1], m.ecoef[4 * ie + 2], m.ecoef[4 * ie + 3]};
+    double p[8];
+    drm_forces(kc, m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m.fdrm[((size_t)s * 16 + k) * m.R + r] = p[k];
+}
+
+// ----------------------------------------------------------- elements ----
+__global__ void __launch_bounds__(256) k_elem64(DevModel m, const double *__restrict__ u,
+                                                const double *__restrict__ um, double *__restrict__ ef) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.ne * m.R) return;
+    int e = (int)(t / m.R), r = (int)(t % m.R);
+    const int4 c = reinterpret_cast<const int4 *>(m.econn)[e];
+    const int cn[4] = {c.x, c.y, c.z, c.w};
+    double ux[4], uy[4], vx[4], vy[4];
+    if (m.R == 1) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            double2 a = reinterpret_cast<const double2 *>(u)[cn[k]];
+            double2 b = reinterpret_cast<const double2 *>(um)[cn[k]];
+            ux[k] = a.x; uy[k] = a.y; vx[k] = b.x; vy[k] = b.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            size_t ix = ((size_t)cn[k] * 2) * m.R + r, iy = ix + m.R;
+            ux[k] = u[ix]; uy[k] = u[iy]; vx[k] = um[ix]; vy[k] = um[iy];
+        }
+    }
+    const double4 kc = reinterpret_cast<const double4 *>(m.ecoef)[e];
+    double fx[4], fy[4];
+    q4_ku<double>(kc.x, kc.y, kc.z, kc.w, ux, uy, fx, fy);
+    double mass = m.emass[e];
+    int ds = m.edamp[e];
+    double lr[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        lr[2 * k] = (m.a3 * ux[k] - m.a1 * vx[k]) * mass;
+        lr[2 * k + 1] = (m.a3 * uy[k] - m.a1 * vy[k]) * mass;
+    }
+    if (ds >= 0) {
+        const double *dv = m.edampv + (size_t)ds * 8;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            lr[2 * k] = lr[2 * k] + m.a2 * dv[2 * k] * vx[k];
+            lr[2 * k + 1] = lr[2 * k + 1] + m.a2 * dv[2 * k + 1] * vy[k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { lr[2 * k] -= fx[k]; lr[2 * k + 1] -= fy[k]; }
+    if (m.R == 1) {
+        double4 *o = reinterpret_cast<double4 *>(ef + (size_t)e * 8);
+        o[0] = make_double4(lr[0], lr[1], lr[2], lr[3]);
+        o[1] = make_double4(lr[4], lr[5], lr[6], lr[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) ef[((size_t)e * 8 + k) * m.R + r] = lr[k];
+    }
+}
+
+// --------------------------------------------------------------- nodes ----
+__global__ void __launch_bounds__(256) k_node64(DevModel m, const double *__restrict__ ef,
+                                                double *__restrict__ unew) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.n_active * m.R) return;
+    int n = (int)(t / m.R), r = (int)(t % m.R);
+    double rx = 0.0, ry = 0.0;
+    for (int q = m.dptr[n]; q < m.dptr[n + 1]; ++q) {
+        int ent = m.dlist[q];
+        double w = (ent & 1) ? 0.5 : 1.0;
+        int sc = ent >> 1;
+        size_t base = ((size_t)(sc >> 2) * 16 + 2 * (sc & 3)) * m.R + r;
+        rx += w * m.fdrm[base];
+        ry += w * m.fdrm[base + m.R];
+    }
+    const int q0 = m.tptr[n], q1 = m.tptr[n + 1];
+    if (m.R == 1) {
+        for (int q = q0; q < q1; ++q) {
+            int ent = __ldg(m.tlist + q);
+            double w = (ent & 1) ? 0.5 : 1.0;
+            int ec = ent >> 1;
+            double2 v = reinterpret_cast<const double2 *>(ef)[(size_t)(ec >> 2) * 4 + (ec & 3)];
+            rx += w * v.x;
+            ry += w * v.y;
+        }
+        double2 im = reinterpret_cast<const double2 *>(m.inv_mfull)[n];
+        reinterpret_cast<double2 *>(unew)[n] = make_double2(rx * im.x, ry * im.y);
+    } else {
+        for (int q = q0; q < q1; ++q) {
+            int ent = __ldg(m.tlist + q);
+            double w = (ent & 1) ? 0.5 : 1.0;
+            int ec = ent >> 1;
+            size_t base = ((size_t)(ec >> 2) * 8 + 2 * (ec & 3)) * m.R + r;
+            rx += w * ef[base];
+            ry += w * ef[base + m.R];
+        }
+        unew[((size_t)n * 2) * m.R + r] = rx * m.inv_mfull[2 * n];
+        unew[((size_t)n * 2 + 1) * m.R + r] = ry * m.inv_mfull[2 * n + 1];
+    }
+}
+
+inline int nblocks(long long work, int threads) { return (int)std::max<long long>(1, (work + threads - 1) / threads); }
+
+int launch_step64(Ctx &c, int par) {
+    DevModel &m = c.dm;
+    double *u = c.u64[par], *um = c.u64[par ^ 1];
+    if (c.opts.variant == EXFEM_VARIANT_REFERENCE_ORDER) {
+        if (f64ref_launch_drm_elem_node(c, par)) { c.err = cudaGetErrorString(cudaGetLastError()); return EXFEM_E_CUDA; }
+    } else {
+        const int T = c.block_threads;
+        if (m.ns > 0) {
+            k_drm<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+            c.launches++;
+            mark(c, "k_drm");
+        }
+        k_elem64<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, u, um, c.ef64);
+        mark(c, "k_elem64");
+        k_node64<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, c.ef64, um);
+        mark(c, "k_node64");
+        c.launches += 2;
+        CK(cudaGetLastError());
+    }
+    if (f64_launch_hang(c, um, 0)) { c.err = cudaGetErrorString(cudaGetLastError()); return EXFEM_E_CUDA; }
+    return EXFEM_OK;
+}
+
+int launch_sample0_64(Ctx &c, int par) {
+    if (f64_launch_hang(c, c.u64[par], 1)) { c.err = cudaGetErrorString(cudaGetLastError()); return EXFEM_E_CUDA; }
+    return EXFEM_OK;
+}
+
+template <typename T>
+int upload(Ctx &c, const std::vector<T> &v, const T **dst) {
+    if (v.empty()) { *dst = nullptr; return EXFEM_OK; }
+    void *p = nullptr;
+    CK(cudaMalloc(&p, v.size() * sizeof(T)));
+    c.allocs.push_back(p);
+    c.bytes += v.size() * sizeof(T);
+    CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    *dst = static_cast<const T *>(p);
+    return EXFEM_OK;
+}
+
+template <typename T>
+int dalloc(Ctx &c, size_t n, T **dst) {
+    void *p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc(&p, n * sizeof(T)));
+    c.allocs.push_back(p);
+    c.bytes += n * sizeof(T);
+    *dst = static_cast<T *>(p);
+    return EXFEM_OK;
+}
+
+#define TRY(x)                   \
+    do {                         \
+        int rc_ = (x);           \
+        if (rc_) return rc_;     \
+    } while (0)
+
+int setup_device(Ctx &c) {
+    Plan &P = c.plan;
+    DevModel &m = c.dm;
+    m.nn = P.nn; m.ne = P.ne; m.R = P.R; m.n_active = P.n_active; m.n_hang = P.n_hang;
+    m.ns = (int)P.s_elem.size(); m.nrecv = P.nrecv; m.nsave = P.nsave; m.io = P.io;
+    m.dt = P.dt; m.a1 = P.a1; m.a2 = P.a2; m.a3 = P.a3;
+    m.worigin_x = P.worigin[0]; m.worigin_y = P.worigin[1];
+    TRY(upload(c, P.econn, &m.econn));
+    TRY(upload(c, P.emass, &m.emass));
+    TRY(upload(c, P.emulam, &m.emulam));
+    TRY(upload(c, P.mfull_int, &m.mfull));
+    TRY(upload(c, P.ownptr, &m.ownptr));
+    TRY(upload(c, P.ownlist, &m.ownlist));
+    TRY(upload(c, P.odptr, &m.odptr));
+    TRY(upload(c, P.odlist, &m.odlist));
+    TRY(upload(c, P.lptr, &m.lptr));
+    TRY(upload(c, P.llist, &m.llist));
+    TRY(upload(c, P.edamp, &m.edamp));
+    TRY(upload(c, P.edampv, &m.edampv));
+    TRY(upload(c, P.tptr, &m.tptr));
+    TRY(upload(c, P.tlist, &m.tlist));
+    TRY(upload(c, P.dptr, &m.dptr));
+    TRY(upload(c, P.dlist, &m.dlist));
+    TRY(upload(c, P.hang, &m.hang));
+    TRY(upload(c, P.s_elem, &m.s_elem));
+    TRY(upload(c, P.s_kind, &m.s_kind));
+    TRY(upload(c, P.rnode, &m.rnode));
+    TRY(upload(c, P.rw, &m.rw));
+    TRY(upload(c, P.rsoil, &m.rsoil));
+    TRY(upload(c, P.rxy, &m.rxy));
+    TRY(upload(c, P.ecoef, &m.ecoef));
+    TRY(upload(c, P.inv_mfull, &m.inv_mfull));
+    std::vector<DevWave> dw(P.R);
+    for (int r = 0; r < P.R; ++r) {
+        const WaveConst &w = P.waves[r];
+        DevWave &d = dw[r];
+        d.kind = w.kind; d.alpha = w.alpha; d.beta = w.beta; d.fp = w.fp;
+        d.sine = w.sine; d.cose = w.cose; d.sinf = w.sinf; d.cosf = w.cosf;
+        d.amp0 = w.amp0; d.wa1 = w.wa1; d.wb1 = w.wb1;
+        for (int k = 0; k < 6; ++k) d.wui[k] = w.wui[k];
+        d.t0 = w.t0;
+    }
+    TRY(upload(c, dw, &m.waves));
+    TRY(dalloc(c, (size_t)std::max(m.ns, 1) * 16 * P.R, &m.fdrm));
+    TRY(dalloc(c, (size_t)P.R * P.nsave * std::max(P.nrecv, 1) * 2, &m.seis));
+    int *ctr = nullptr;
+    TRY(dalloc(c, 4, &ctr));
+    m.d_step = ctr;
+    m.d_flag = ctr + 1;
+    m.d_blocks = reinterpret_cast<unsigned *>(ctr + 2);
+    return EXFEM_OK;
+}
+
+int alloc_fp64(Ctx &c) {
+    const Plan &P = c.plan;
+    size_t nst = (size_t)P.nn * 2 * P.R;
+    TRY(dalloc(c, nst, &c.u64[0]));
+    TRY(dalloc(c, nst, &c.u64[1]));
+    TRY(dalloc(c, (size_t)P.ne * 8 * P.R, &c.ef64));
+    return EXFEM_OK;
+}
+
+void free_all(Ctx &c) {
+    if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+    for (void *p : c.allocs) cudaFree(p);
+    c.allocs.clear();
+    if (c.stream) { cudaStreamDestroy(c.stream); c.stream = nullptr; }
+}
+
+int launch_step(Ctx &c, int par) {
+    return c.precision == EXFEM_FP64 ? launch_step64(c, par) : f32_launch_step(c, par);
+}
+
+// Capture `g` steps starting at parity 0 into a graph (g even keeps parity).
+int capture_graph(Ctx &c, int g) {
+    if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    long long before = c.launches;
+    int par = 0, rc = EXFEM_OK;
+    for (int i = 0; i < g && rc == EXFEM_OK; ++i) {
+        rc = launch_step(c, par);
+        par ^= 1;
+    }
+    cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
+    c.launches = before;   // captured launches are counted on replay
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) { c.err = std::string("graph capture: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    e = cudaGraphInstantiate(&c.graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { c.err = std::string("graph instantiate: ") + cudaGetErrorString(e); c.graph = nullptr; return EXFEM_E_CUDA; }
+    c.graph_steps = g;
+    return EXFEM_OK;
+}
+
+int launches_per_step(const Ctx &c) {
+    if (c.precision == EXFEM_FP64) return (c.dm.ns > 0 ? 1 : 0) + 3;   // drm, elem, node, hang
+    return (c.dm.ns > 0 ? 1 : 0) + 2;
+}
+
+// Device side of exfem_gpu_create: stream, uploads, state buffers.
+int create_device(Ctx &c, const exfem_mesh &mesh) {
+    CK(cudaSetDevice(c.device));
+    CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    // node coordinates in internal order (free field at DRM corners)
+    std::vector<double> nxy(2 * (size_t)c.plan.nn);
+    for (int i = 0; i < c.plan.nn; ++i) {
+        int rn = c.plan.ref_of_node[i];
+        nxy[2 * (size_t)i] = mesh.nodes[2 * (size_t)rn];
+        nxy[2 * (size_t)i + 1] = mesh.nodes[2 * (size_t)rn + 1];
+    }
+    TRY(upload(c, nxy, &c.dm.nxy));
+    TRY(setup_device(c));
+    c.block_threads = c.opts.block_threads > 0 ? c.opts.block_threads : 128;
+    TRY(c.precision == EXFEM_FP64 ? alloc_fp64(c) : f32_alloc(c));
+    CK(cudaStreamSynchronize(c.stream));
+    return EXFEM_OK;
+}
+
+}  // namespace
+
+namespace exfem {
+void mark(Ctx &c, const char *kernel) {
+    if (!c.prof_on) return;
+    cudaEvent_t ev = nullptr;
+    if (cudaEventCreate(&ev) != cudaSuccess) return;
+    cudaEventRecord(ev, c.stream);
+    c.marks.push_back({kernel, ev});
+}
+}  // namespace exfem
+
+struct exfem_ctx : Ctx {};
+
+extern "C" {
+
+void exfem_gpu_default_opts(exfem_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = EXFEM_FP64;
+    o->device = 0;
+    o->use_graph = 1;
+    o->graph_steps = 0;
+    o->block_threads = 0;
+    o->rhs_per_thread = 0;
+    o->reorder = 1;
+    o->check_every = 0;
+    o->variant = EXFEM_VARIANT_REFERENCE_ORDER;
+}
+
+int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts, exfem_ctx **out) {
+    g_create_err.clear();
+    if (!out || !mesh || !prob) { g_create_err = "NULL argument"; return EXFEM_E_ARG; }
+    *out = nullptr;
+    exfem_opts o;
+    if (opts) o = *opts;
+    else exfem_gpu_default_opts(&o);
+    if (o.precision != EXFEM_FP64 && o.precision != EXFEM_FP32_KAHAN) { g_create_err = "unknown precision"; return EXFEM_E_ARG; }
+    if (o.variant != EXFEM_VARIANT_REFERENCE_ORDER && o.variant != EXFEM_VARIANT_CLOSED_FORM) {
+        g_create_err = "unknown kernel variant";
+        return EXFEM_E_ARG;
+    }
+    if (o.block_threads < 0 || o.block_threads > 1024 || (o.block_threads % 32) != 0) {
+        g_create_err = "block_threads must be a multiple of 32 in [0, 1024]";
+        return EXFEM_E_ARG;
+    }
+    exfem_ctx *c = nullptr;
+    try {
+        c = new exfem_ctx();
+    } catch (const std::bad_alloc &) {
+        g_create_err = "host allocation failed";
+        return EXFEM_E_NOMEM;
+    }
+    c->opts = o;
+    c->precision = o.precision;
+    c->device = o.device;
+    int rc;
+    try {
+        rc = build_plan(*mesh, *prob, o.reorder != 0, c->plan, c->err);
+    } catch (const std::bad_alloc &) {
+        rc = EXFEM_E_NOMEM;
+        c->err = "host allocation failed while preparing the model";
+    }
+    if (rc) { g_create_err = c->err; delete c; return rc; }
+    rc = create_device(*c, *mesh);
+    if (rc) {
+        if (rc == EXFEM_E_CUDA && c->err.find("out of memory") != std::string::npos) rc = EXFEM_E_NOMEM;
+        g_create_err = c->err;
+        free_all(*c);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return EXFEM_OK;
+}
+
+int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out) {
+    if (!ctx) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    CK(cudaSetDevice(c.device));
+    DevModel &m = c.dm;
+    if (c.precision == EXFEM_FP64) {
+        size_t nst = (size_t)c.plan.nn * 2 * c.plan.R;
+        CK(cudaMemsetAsync(c.u64[0], 0, nst * sizeof(double), c.stream));
+        CK(cudaMemsetAsync(c.u64[1], 0, nst * sizeof(double), c.stream));
+    } else {
+        int rc = f32_init(c);
+        if (rc) return rc;
+    }
+    CK(cudaMemsetAsync(m.seis, 0, sizeof(double) * (size_t)c.plan.R * c.plan.nsave * std::max(c.plan.nrecv, 1) * 2,
+                       c.stream));
+    CK(cudaMemsetAsync(m.d_step, 0, 4 * sizeof(int), c.stream));
+    c.parity = 0;
+    c.steps_done = 0;
+    int rc = c.precision == EXFEM_FP64 ? launch_sample0_64(c, 0) : f32_launch_sample0(c, 0);
+    if (rc) return rc;
+    if (mfull_out) std::memcpy(mfull_out, c.plan.mfull_ref.data(), sizeof(double) * c.plan.mfull_ref.size());
+    c.inited = true;
+    return EXFEM_OK;
+}
+
+int exfem_gpu_run(exfem_ctx *ctx, int nsteps) {
+    if (!ctx) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    if (!c.inited) { c.err = "exfem_gpu_run before exfem_gpu_init_explicit"; return EXFEM_E_STATE; }
+    if (nsteps < 0 || nsteps > c.plan.nsteps - c.steps_done) {
+        c.err = "nsteps exceeds the steps left in the problem";
+        return EXFEM_E_ARG;
+    }
+    CK(cudaSetDevice(c.device));
+    int left = nsteps;
+    if (c.opts.use_graph) {
+        int g = c.opts.graph_steps > 0 ? c.opts.graph_steps : 16;
+        g += g & 1;
+        if (left >= g) {
+            if (!c.graph || c.graph_steps != g) {
+                int rc = capture_graph(c, g);
+                if (rc) return rc;
+            }
+            // the graph was captured from parity 0: align first
+            if (c.parity == 1) {
+                int rc = launch_step(c, c.parity);
+                if (rc) return rc;
+                c.parity ^= 1;
+                --left;
+                c.steps_done++;
+            }
+            while (left >= g) {
+                CK(cudaGraphLaunch(c.graph, c.stream));
+                c.launches += (long long)g * launches_per_step(c);
+                left -= g;
+                c.steps_done += g;
+            }
+        }
+    }
+    while (left > 0) {
+        int rc = launch_step(c, c.parity);
+        if (rc) return rc;
+        c.parity ^= 1;
+        --left;
+        c.steps_done++;
+    }
+    return EXFEM_OK;
+}
+
+int exfem_gpu_sync(exfem_ctx *ctx) {
+    if (!ctx) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    CK(cudaSetDevice(c.device));
+    CK(cudaStreamSynchronize(c.stream));
+    int flag = 0;
+    CK(cudaMemcpy(&flag, c.dm.d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
+    if (flag & 2) { c.err = "a bounded device wait timed out"; return EXFEM_E_TIMEOUT; }
+    return EXFEM_OK;
+}
+
+int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
+    if (!ctx || !u) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    const Plan &P = c.plan;
+    if (rhs < 0 || rhs >= P.R || n < (size_t)2 * P.nn) { c.err = "bad rhs or buffer too small"; return EXFEM_E_ARG; }
+    CK(cudaSetDevice(c.device));
+    CK(cudaStreamSynchronize(c.stream));
+    std::vector<double> in;
+    if (c.precision == EXFEM_FP64) {
+        std::vector<double> all((size_t)P.nn * 2 * P.R);
+        CK(cudaMemcpy(all.data(), c.u64[c.parity], all.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        in.resize((size_t)P.nn * 2);
+        for (int i = 0; i < P.nn; ++i)
+            for (int d = 0; d < 2; ++d) in[2 * (size_t)i + d] = all[((size_t)i * 2 + d) * P.R + rhs];
+    } else {
+        int rc = f32_get_u(c, rhs, in);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < P.nn; ++i) {
+        int rn = P.ref_of_node[i];
+        u[2 * (size_t)rn] = in[2 * (size_t)i];
+        u[2 * (size_t)rn + 1] = in[2 * (size_t)i + 1];
+    }
+    return EXFEM_OK;
+}
+
+int exfem_gpu_get_seismograms(exfem_ctx *ctx, double *out, size_t cap, int *nsaved) {
+    if (!ctx) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    const Plan &P = c.plan;
+    size_t need = (size_t)P.R * P.nsave * P.nrecv * 2;
+    if (nsaved) *nsaved = c.steps_done / P.io + 1;
+    if (!out) return EXFEM_OK;
+    if (cap < need) { c.err = "seismogram buffer too small"; return EXFEM_E_ARG; }
+    CK(cudaSetDevice(c.device));
+    CK(cudaStreamSynchronize(c.stream));
+    if (need) CK(cudaMemcpy(out, c.dm.seis, need * sizeof(double), cudaMemcpyDeviceToHost));
+    return EXFEM_OK;
+}
+
+int exfem_gpu_run_timed(exfem_ctx *ctx, int nsteps, double *ms) {
+    if (!ctx || !ms) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    CK(cudaSetDevice(c.device));
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    cudaEventRecord(a, c.stream);
+    int rc = exfem_gpu_run(ctx, nsteps);
+    cudaEventRecord(b, c.stream);
+    cudaError_t e = cudaEventSynchronize(b);
+    float f = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    *ms = f;
+    return EXFEM_OK;
+}
+
+int exfem_gpu_profile_kernels(exfem_ctx *ctx, int nsteps, double *ms_out, const char **names_out, int cap) {
+    if (!ctx || !ms_out || !names_out || cap <= 0) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    if (!c.inited) { c.err = "profile before exfem_gpu_init_explicit"; return EXFEM_E_STATE; }
+    if (nsteps < 1 || nsteps > c.plan.nsteps - c.steps_done) { c.err = "nsteps exceeds the steps left"; return EXFEM_E_ARG; }
+    CK(cudaSetDevice(c.device));
+    CK(cudaStreamSynchronize(c.stream));
+    c.prof_on = true;
+    c.marks.clear();
+    mark(c, "start");
+    int rc = EXFEM_OK;
+    for (int i = 0; i < nsteps && rc == EXFEM_OK; ++i) {
+        rc = launch_step(c, c.parity);
+        c.parity ^= 1;
+        c.steps_done++;
+    }
+    c.prof_on = false;
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    std::vector<std::string> names;
+    std::vector<double> tot;
+    std::vector<int> cnt;
+    for (size_t k = 1; k < c.marks.size() && e == cudaSuccess; ++k) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, c.marks[k - 1].second, c.marks[k].second);
+        std::string n = c.marks[k].first;
+        size_t j = 0;
+        while (j < names.size() && names[j] != n) ++j;
+        if (j == names.size()) { names.push_back(n); tot.push_back(0); cnt.push_back(0); }
+        tot[j] += f;
+        cnt[j]++;
+    }
+    for (auto &pr : c.marks) cudaEventDestroy(pr.second);
+    c.marks.clear();
+    if (rc) return rc;
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    int n = (int)std::min<size_t>(names.size(), (size_t)cap);
+    static thread_local std::vector<std::string> keep;
+    keep = names;
+    for (int k = 0; k < n; ++k) {
+        ms_out[k] = tot[k] / cnt[k];
+        names_out[k] = keep[k].c_str();
+    }
+    return n;
+}
+
+int exfem_gpu_steps_done(const exfem_ctx *ctx) { return ctx ? ctx->steps_done : 0; }
+long long exfem_gpu_launch_count(const exfem_ctx *ctx) { return ctx ? ctx->launches : 0; }
+size_t exfem_gpu_device_bytes(const exfem_ctx *ctx) { return ctx ? ctx->bytes : 0; }
+
+size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts) {
+    if (!mesh || !prob) return 0;
+    size_t nn = (size_t)std::max(mesh->nnodes, 0), ne = (size_t)std::max(mesh->nelems, 0);
+    size_t R = (size_t)std::max(prob->nrhs, 1);
+    size_t nsave = (size_t)(prob->io_interval > 0 ? prob->nsteps / prob->io_interval + 1 : 1);
+    bool f64 = !opts || opts->precision == EXFEM_FP64;
+    size_t b = ne * (16 + 32 + 16 + 8 + 4) + nn * (16 + 8 + 16 + 4 * 12) + (size_t)prob->nhanging * 12 * 8;
+    b += R * nsave * (size_t)prob->nrecv * 16 + (size_t)prob->nseismic * (8 * 8 * R + 8);
+    if (f64) b += R * (nn * 32 + ne * 64);
+    else b += R * nn * 24 + nn * 24;
+    return b + (1u << 20);
+}
+
+const char *exfem_gpu_last_error(const exfem_ctx *ctx) {
+    if (!ctx) return g_create_err.c_str();
+    return ctx->err.c_str();
+}
+
+void exfem_gpu_destroy(exfem_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_all(*ctx);
+    delete ctx;
+}
+
+}  // extern "C"

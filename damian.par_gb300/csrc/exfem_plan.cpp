@@ -1,0 +1,439 @@
+// exfem_plan.cpp — host-side preparation of the device model (see exfem_plan.h).
+#include "exfem_plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace exfem {
+
+namespace {
+constexpr double U_PI = 3.14159265358979323846;
+constexpr double U_TOL = 1.0e-9;
+const double F_WANGZERO = (double)0.0001f;   // pwaves.f90:8 (single literal in a real*8)
+inline bool realunder(double a, double b) { return (a - b) < -U_TOL; }
+inline bool realover(double a, double b) { return (a - b) > U_TOL; }
+
+uint64_t spread21(uint64_t v) {
+    v &= 0x1fffff;
+    v = (v | v << 32) & 0x1f00000000ffffULL;
+    v = (v | v << 16) & 0x1f0000ff0000ffULL;
+    v = (v | v << 8) & 0x100f00f00f00f00fULL;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+    v = (v | v << 2) & 0x1249249249249249ULL;
+    return v;
+}
+
+struct Morton {
+    double x0, y0, sx, sy;
+    Morton(const std::vector<double> &xs, const std::vector<double> &ys) {
+        double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+        for (size_t i = 0; i < xs.size(); ++i) {
+            xmin = std::min(xmin, xs[i]); xmax = std::max(xmax, xs[i]);
+            ymin = std::min(ymin, ys[i]); ymax = std::max(ymax, ys[i]);
+        }
+        x0 = xmin; y0 = ymin;
+        double span = std::max(std::max(xmax - xmin, ymax - ymin), 1e-30);
+        sx = sy = 2097151.0 / span;
+    }
+    uint64_t key(double x, double y) const {
+        uint64_t ix = (uint64_t)std::llround((x - x0) * sx), iy = (uint64_t)std::llround((y - y0) * sy);
+        return spread21(ix) | (spread21(iy) << 1);
+    }
+};
+}  // namespace
+
+// initplanewaves (pwaves.f90:16-98), kept in the order of the reference's
+// arithmetic; EXFEM_E_UNSUPPORTED where the reference exits.
+int init_wave_const(const exfem_wave &w, double alpha, double beta, WaveConst &o, std::string &err) {
+    o = WaveConst();
+    o.kind = w.kind;
+    o.alpha = alpha;
+    o.beta = beta;
+    o.freq = w.freq;
+    o.fp = w.freq * U_PI;
+    o.t0 = w.t0;
+    if (!(alpha > 0) || !(beta > 0) || !(w.freq > 0) || !std::isfinite(w.angle) || !std::isfinite(w.amp)) {
+        err = "wave parameters must be finite with positive velocities and frequency";
+        return EXFEM_E_ARG;
+    }
+    double wa = 0, wb = 0;
+    if (w.kind == EXFEM_WAVE_P) {
+        double e = w.angle, a = w.amp;
+        o.sine = std::sin(e);
+        o.sinf = o.sine * (beta / alpha);
+        double f = std::asin(o.sinf);
+        o.cose = std::cos(e);
+        o.cosf = std::cos(f);
+        if (o.cose < F_WANGZERO) {
+            err = "P wave at grazing incidence is not supported (pwaves.f90:32-35)";
+            return EXFEM_E_UNSUPPORTED;
+        } else if (std::fabs(o.sine) < F_WANGZERO) {
+            wa = a; o.wa1 = -wa; o.wb1 = 0.0; o.cose = 1; o.sine = 0;
+        } else {
+            double sin2e = std::sin(2 * e), sin2f = std::sin(2 * f), cos2f = std::cos(2 * f), r = alpha / beta;
+            wa = a;
+            o.wa1 = (sin2e * sin2f - (r * r) * (cos2f * cos2f));
+            o.wa1 = o.wa1 / (sin2e * sin2f + (r * r) * (cos2f * cos2f));
+            o.wa1 = o.wa1 * a;
+            o.wb1 = -(2 * r * sin2e * cos2f);
+            o.wb1 = o.wb1 / (sin2e * sin2f + (r * r) * (cos2f * cos2f));
+            o.wb1 = o.wb1 * a;
+        }
+        o.amp0 = wa;
+        o.wui[0] = o.sine; o.wui[1] = -o.cose;
+        o.wui[2] = o.sine; o.wui[3] = o.cose;
+        o.wui[4] = -o.cosf; o.wui[5] = o.sinf;
+    } else if (w.kind == EXFEM_WAVE_SV) {
+        double f = w.angle, b = w.amp;
+        o.sinf = std::sin(f);
+        double fcr = std::asin(beta / alpha);
+        o.sine = o.sinf * (alpha / beta);
+        double e = std::asin(o.sine);
+        o.cose = std::cos(e);
+        o.cosf = std::cos(f);
+        if (std::fabs(o.sinf) < F_WANGZERO) {
+            wb = b; o.wb1 = -wb; o.wa1 = 0.0; o.cosf = 1; o.sinf = 0;
+        } else if ((fcr - f) > F_WANGZERO) {
+            double sin2e = std::sin(2 * e), sin2f = std::sin(2 * f), cos2f = std::cos(2 * f), r = alpha / beta;
+            wb = b;
+            o.wb1 = (sin2e * sin2f - (r * r) * (cos2f * cos2f));
+            o.wb1 = o.wb1 / (sin2e * sin2f + (r * r) * (cos2f * cos2f));
+            o.wb1 = o.wb1 * b;
+            o.wa1 = r * std::sin(4.0 * f);
+            o.wa1 = o.wa1 / (sin2e * sin2f + (r * r) * (cos2f * cos2f));
+            o.wa1 = o.wa1 * b;
+        } else {
+            err = "SV wave at or beyond the critical angle asin(vs/vp) is not supported (pwaves.f90:87-89)";
+            return EXFEM_E_UNSUPPORTED;
+        }
+        o.amp0 = wb;
+        o.wui[0] = o.cosf; o.wui[1] = o.sinf;
+        o.wui[2] = o.sine; o.wui[3] = o.cose;
+        o.wui[4] = -o.cosf; o.wui[5] = o.sinf;
+    } else {
+        err = "wave kind must be EXFEM_WAVE_P or EXFEM_WAVE_SV";
+        return EXFEM_E_ARG;
+    }
+    return EXFEM_OK;
+}
+
+int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &P, std::string &err) {
+    const int nn = mesh.nnodes, ne = mesh.nelems;
+    if (nn <= 0 || ne <= 0 || !mesh.eptr || !mesh.eind || !mesh.ediv || !mesh.nodes || !mesh.ematprop) {
+        err = "mesh arrays missing or empty";
+        return EXFEM_E_ARG;
+    }
+    if (prob.nmat <= 0 || !prob.matconst || !prob.absorbing || prob.nrhs <= 0 || !prob.waves) {
+        err = "problem arrays missing (matconst/absorbing/waves)";
+        return EXFEM_E_ARG;
+    }
+    if (!(prob.deltat > 0) || prob.nsteps < 0 || prob.io_interval < 1) {
+        err = "deltat must be > 0, nsteps >= 0 and io_interval >= 1";
+        return EXFEM_E_ARG;
+    }
+    if (prob.nhanging < 0 || prob.nseismic < 0 || prob.nrecv < 0 ||
+        (prob.nhanging > 0 && !prob.hanging) || (prob.nseismic > 0 && !prob.seismic) ||
+        (prob.nrecv > 0 && (!prob.recv_xy || !prob.recv_elem))) {
+        err = "hanging/seismic/receiver arrays inconsistent with their counts";
+        return EXFEM_E_ARG;
+    }
+    if ((long long)ne * 8 >= (1LL << 30) || nn >= (1 << 29)) {
+        err = "mesh too large for 32-bit gather entries";
+        return EXFEM_E_ARG;
+    }
+    P.nn = nn; P.ne = ne; P.R = prob.nrhs;
+    P.dt = prob.deltat;
+    // setupconstants (explicit.f90:72-77)
+    P.a1 = 1.0 / (P.dt * P.dt);
+    P.a2 = 1.0 / (2.0 * P.dt);
+    P.a3 = 2.0 * P.a1;
+    P.nsteps = prob.nsteps;
+    P.io = prob.io_interval;
+    P.nsave = prob.nsteps / prob.io_interval + 1;
+    P.worigin[0] = prob.worigin[0];
+    P.worigin[1] = prob.worigin[1];
+
+    // ---- corners (elemallnhnodes, model.f90:163-174) and validation
+    if (mesh.eptr[0] != 1) { err = "eptr[0] must be 1 (1-based CSR)"; return EXFEM_E_MESH; }
+    std::vector<int> corner_ref((size_t)ne * 4);
+    for (int e = 0; e < ne; ++e) {
+        int b = mesh.eptr[e] - 1, t = mesh.eptr[e + 1] - 1;
+        if (t <= b || t - b > 8) { err = "element " + std::to_string(e + 1) + " has a bad CSR row"; return EXFEM_E_MESH; }
+        int k = 0;
+        for (int j = b; j < t; ++j) {
+            int v = mesh.eind[j];
+            if (v < 1 || v > nn) { err = "eind out of range in element " + std::to_string(e + 1); return EXFEM_E_MESH; }
+            if (!mesh.ediv[j]) { if (k < 4) corner_ref[(size_t)e * 4 + k] = v - 1; ++k; }
+        }
+        if (k != 4) {
+            err = "element " + std::to_string(e + 1) + " has " + std::to_string(k) + " non-hanging nodes (model.f90:166-171)";
+            return EXFEM_E_MESH;
+        }
+        int m = mesh.ematprop[e];
+        if (m < 1 || m > prob.nmat) { err = "ematprop out of range in element " + std::to_string(e + 1); return EXFEM_E_MESH; }
+    }
+    // ---- hanging entries
+    std::vector<int> hang_of(nn, -1);   // reference node -> hanging entry
+    for (int i = 0; i < prob.nhanging; ++i) {
+        int h = prob.hanging[3 * i] - 1, a = prob.hanging[3 * i + 1] - 1, b = prob.hanging[3 * i + 2] - 1;
+        if (h < 0 || h >= nn || a < 0 || a >= nn || b < 0 || b >= nn || h == a || h == b) {
+            err = "hanging entry " + std::to_string(i + 1) + " out of range";
+            return EXFEM_E_MESH;
+        }
+        if (hang_of[h] >= 0) { err = "node " + std::to_string(h + 1) + " listed twice as hanging"; return EXFEM_E_MESH; }
+        hang_of[h] = i;
+    }
+    for (int i = 0; i < prob.nhanging; ++i) {
+        int a = prob.hanging[3 * i + 1] - 1, b = prob.hanging[3 * i + 2] - 1;
+        if (hang_of[a] >= 0 || hang_of[b] >= 0) {
+            // a 2:1-balanced quadtree (mesh_utils.f90:124-135) never anchors a
+            // hanging node on another hanging node
+            err = "chained hanging nodes (an anchor is itself hanging) are not supported";
+            return EXFEM_E_UNSUPPORTED;
+        }
+    }
+    // ---- internal numbering (Morton order; active nodes first, hanging last)
+    std::vector<double> xs(nn), ys(nn);
+    for (int i = 0; i < nn; ++i) { xs[i] = mesh.nodes[2 * i]; ys[i] = mesh.nodes[2 * i + 1]; }
+    std::vector<int> order(nn);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<uint64_t> keys(nn, 0);
+    Morton mort(xs, ys);
+    if (reorder)
+        for (int i = 0; i < nn; ++i) keys[i] = mort.key(xs[i], ys[i]);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        bool ha = hang_of[a] >= 0, hb = hang_of[b] >= 0;
+        if (ha != hb) return !ha;
+        if (ha) return hang_of[a] < hang_of[b];   // hanging entry i -> internal n_active + i
+        return keys[a] < keys[b];
+    });
+    P.ref_of_node = order;
+    P.node_of_ref.assign(nn, -1);
+    for (int i = 0; i < nn; ++i) P.node_of_ref[order[i]] = i;
+    P.n_hang = prob.nhanging;
+    P.n_active = nn - P.n_hang;
+
+    std::vector<int> eorder(ne);
+    std::iota(eorder.begin(), eorder.end(), 0);
+    if (reorder) {
+        std::vector<uint64_t> ek(ne);
+        for (int e = 0; e < ne; ++e) {
+            const int *c = &corner_ref[(size_t)e * 4];
+            double cx = 0.25 * (xs[c[0]] + xs[c[1]] + xs[c[2]] + xs[c[3]]);
+            double cy = 0.25 * (ys[c[0]] + ys[c[1]] + ys[c[2]] + ys[c[3]]);
+            ek[e] = mort.key(cx, cy);
+        }
+        std::stable_sort(eorder.begin(), eorder.end(), [&](int a, int b) { return ek[a] < ek[b]; });
+    }
+    P.ref_of_elem = eorder;
+    std::vector<int> elem_of_ref(ne);
+    for (int e = 0; e < ne; ++e) elem_of_ref[eorder[e]] = e;
+
+    // ---- per-element data (internal order)
+    P.econn.resize((size_t)ne * 4);
+    P.ecoef.resize((size_t)ne * 4);
+    P.ecoef32.resize((size_t)ne * 4);
+    P.emass.resize(ne);
+    P.emulam.resize((size_t)ne * 2);
+    P.edamp.assign(ne, -1);
+    P.edampv.clear();
+    std::vector<double> eh(ne);
+    for (int ie = 0; ie < ne; ++ie) {
+        int e = eorder[ie];
+        const int *c = &corner_ref[(size_t)e * 4];
+        for (int k = 0; k < 4; ++k) P.econn[(size_t)ie * 4 + k] = P.node_of_ref[c[k]];
+        const double *mc = &prob.matconst[5 * (mesh.ematprop[e] - 1)];
+        double mu = mc[0], lam = mc[1], rho = mc[2], vp = mc[3], vs = mc[4];
+        double h = ys[c[2]] - ys[c[0]];   // elength (model.f90:112-118)
+        if (!(h > 0) || !(rho > 0)) {
+            err = "element " + std::to_string(e + 1) + " has non-positive length or density";
+            return EXFEM_E_MESH;
+        }
+        eh[ie] = h;
+        P.emulam[(size_t)ie * 2] = mu;
+        P.emulam[(size_t)ie * 2 + 1] = lam;
+        P.ecoef[(size_t)ie * 4 + 0] = (lam + 2.0 * mu) / 4.0;
+        P.ecoef[(size_t)ie * 4 + 1] = lam / 4.0;
+        P.ecoef[(size_t)ie * 4 + 2] = mu / 4.0;
+        P.ecoef[(size_t)ie * 4 + 3] = (lam + 3.0 * mu) / 12.0;
+        for (int k = 0; k < 4; ++k) P.ecoef32[(size_t)ie * 4 + k] = (float)P.ecoef[(size_t)ie * 4 + k];
+        double scl = h / 2.0;
+        P.emass[ie] = (scl * scl) * rho;   // calcm (formulation.f90:250-254)
+        double damping[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        bool any = false;
+        for (int k = 0; k < 4; ++k) {   // getdampingof + lysmer (model.f90:585-604)
+            int ab = prob.absorbing[c[k]];
+            if (ab == 1 || ab == 2) {
+                double r0 = vp * rho * h, r1 = vs * rho * h;
+                if (ab == 1) { damping[2 * k] = r1; damping[2 * k + 1] = r0; }
+                else { damping[2 * k] = r0; damping[2 * k + 1] = r1; }
+                any = true;
+            }
+        }
+        if (any) {
+            P.edamp[ie] = (int)(P.edampv.size() / 8);
+            P.edampv.insert(P.edampv.end(), damping, damping + 8);
+        }
+    }
+    // ---- m_full (init_explicit, explicit.f90:95-106) in reference order
+    P.mfull_ref.assign((size_t)2 * nn, 0.0);
+    for (int e = 0; e < ne; ++e) {
+        int ie = elem_of_ref[e];
+        const int *c = &corner_ref[(size_t)e * 4];
+        double mass = P.emass[ie];
+        const double *dv = P.edamp[ie] >= 0 ? &P.edampv[(size_t)P.edamp[ie] * 8] : nullptr;
+        for (int k = 0; k < 8; ++k) {
+            double damping = dv ? dv[k] : 0.0;
+            size_t d = (size_t)c[k / 2] * 2 + (k & 1);
+            P.mfull_ref[d] = P.mfull_ref[d] + (P.a2 * damping + P.a1 * mass);
+        }
+    }
+    for (int i = 0; i < prob.nhanging; ++i) {   // sum_reactanchors, halving form
+        int h = prob.hanging[3 * i] - 1, a = prob.hanging[3 * i + 1] - 1, b = prob.hanging[3 * i + 2] - 1;
+        for (int k = 0; k < 2; ++k) {
+            double red = P.mfull_ref[2 * h + k] / 2.0;
+            P.mfull_ref[2 * a + k] += red;
+            P.mfull_ref[2 * b + k] += red;
+        }
+    }
+    P.inv_mfull.resize((size_t)2 * P.n_active);
+    P.mfull_int.resize((size_t)2 * P.n_active);
+    for (int n = 0; n < P.n_active; ++n)
+        for (int k = 0; k < 2; ++k) {
+            double m = P.mfull_ref[(size_t)P.ref_of_node[n] * 2 + k];
+            if (!(m > 0)) { err = "non-positive lumped mass at node " + std::to_string(P.ref_of_node[n] + 1); return EXFEM_E_MESH; }
+            P.inv_mfull[(size_t)2 * n + k] = 1.0 / m;
+            P.mfull_int[(size_t)2 * n + k] = m;
+        }
+    // ---- own incidences per node (internal ids), element order
+    P.ownptr.assign(nn + 1, 0);
+    for (int ie = 0; ie < ne; ++ie)
+        for (int k = 0; k < 4; ++k) P.ownptr[P.econn[(size_t)ie * 4 + k] + 1]++;
+    for (int i = 0; i < nn; ++i) P.ownptr[i + 1] += P.ownptr[i];
+    P.ownlist.resize(P.ownptr[nn]);
+    {
+        std::vector<int> fill(P.ownptr.begin(), P.ownptr.end() - 1);
+        for (int e = 0; e < ne; ++e) {   // reference element order
+            int ie = elem_of_ref[e];
+            for (int k = 0; k < 4; ++k) P.ownlist[fill[P.econn[(size_t)ie * 4 + k]]++] = ie * 4 + k;
+        }
+    }
+    for (int i = 0; i < nn; ++i)
+        if (P.ownptr[i + 1] == P.ownptr[i]) {
+            err = "node " + std::to_string(P.ref_of_node[i] + 1) + " is not a non-hanging corner of any element";
+            return EXFEM_E_MESH;
+        }
+    // ---- hanging entries (internal) and per-anchor links
+    P.hang.resize((size_t)3 * P.n_hang);
+    std::vector<std::vector<std::pair<int, int>>> links(P.n_active);   // anchor -> (h, other anchor)
+    for (int i = 0; i < prob.nhanging; ++i) {
+        int h = P.node_of_ref[prob.hanging[3 * i] - 1];
+        int a = P.node_of_ref[prob.hanging[3 * i + 1] - 1];
+        int b = P.node_of_ref[prob.hanging[3 * i + 2] - 1];
+        P.hang[3 * (size_t)i] = h; P.hang[3 * (size_t)i + 1] = a; P.hang[3 * (size_t)i + 2] = b;
+        links[a].push_back({h, b});
+        links[b].push_back({h, a});
+    }
+    P.lptr.assign(P.n_active + 1, 0);
+    P.llist.clear();
+    for (int n = 0; n < P.n_active; ++n) {
+        for (auto &pr : links[n]) { P.llist.push_back(pr.first); P.llist.push_back(pr.second); }
+        P.lptr[n + 1] = (int)(P.llist.size() / 2);
+    }
+    // ---- gather lists of active nodes: own terms, then linked hanging terms at 1/2
+    P.tptr.assign(P.n_active + 1, 0);
+    P.tlist.clear();
+    P.tlist.reserve(P.ownlist.size() + 8 * P.n_hang);
+    for (int n = 0; n < P.n_active; ++n) {
+        for (int q = P.ownptr[n]; q < P.ownptr[n + 1]; ++q) P.tlist.push_back(P.ownlist[q] << 1);
+        for (auto &pr : links[n])
+            for (int q = P.ownptr[pr.first]; q < P.ownptr[pr.first + 1]; ++q) P.tlist.push_back((P.ownlist[q] << 1) | 1);
+        P.tptr[n + 1] = (int)P.tlist.size();
+    }
+    // ---- per-node lumped mass / damping (internal), for the FP32 increment form
+    P.nmass.assign(nn, 0.0);
+    P.ndamp.assign((size_t)2 * nn, 0.0);
+    for (int ie = 0; ie < ne; ++ie) {
+        const double *dv = P.edamp[ie] >= 0 ? &P.edampv[(size_t)P.edamp[ie] * 8] : nullptr;
+        for (int k = 0; k < 4; ++k) {
+            int x = P.econn[(size_t)ie * 4 + k];
+            P.nmass[x] += P.emass[ie];
+            if (dv) { P.ndamp[2 * (size_t)x] += dv[2 * k]; P.ndamp[2 * (size_t)x + 1] += dv[2 * k + 1]; }
+        }
+    }
+    // ---- DRM slots (wave_elems output, model.f90:1015-1045)
+    P.s_elem.resize(prob.nseismic);
+    P.s_kind.resize(prob.nseismic);
+    std::vector<std::vector<int>> dl(P.n_active);
+    for (int s = 0; s < prob.nseismic; ++s) {
+        int e = prob.seismic[2 * s] - 1, kind = prob.seismic[2 * s + 1];
+        if (e < 0 || e >= ne || !(kind == 1 || kind == 2 || kind == 4 || kind == 5 || kind == 6)) {
+            err = "seismic entry " + std::to_string(s + 1) + " invalid";
+            return EXFEM_E_MESH;
+        }
+        int ie = elem_of_ref[e];
+        P.s_elem[s] = ie;
+        P.s_kind[s] = kind;
+        for (int k = 0; k < 4; ++k) {
+            int x = P.econn[(size_t)ie * 4 + k];
+            int ent = (s * 4 + k) << 1;
+            if (x < P.n_active) dl[x].push_back(ent);
+            else {
+                int hi = hang_of[P.ref_of_node[x]];
+                dl[P.node_of_ref[prob.hanging[3 * hi + 1] - 1]].push_back(ent | 1);
+                dl[P.node_of_ref[prob.hanging[3 * hi + 2] - 1]].push_back(ent | 1);
+            }
+        }
+    }
+    P.odptr.assign(nn + 1, 0);
+    for (int s = 0; s < prob.nseismic; ++s)
+        for (int k = 0; k < 4; ++k) P.odptr[P.econn[(size_t)P.s_elem[s] * 4 + k] + 1]++;
+    for (int i = 0; i < nn; ++i) P.odptr[i + 1] += P.odptr[i];
+    P.odlist.resize(P.odptr[nn]);
+    {
+        std::vector<int> fill(P.odptr.begin(), P.odptr.end() - 1);
+        for (int s = 0; s < prob.nseismic; ++s)
+            for (int k = 0; k < 4; ++k) P.odlist[fill[P.econn[(size_t)P.s_elem[s] * 4 + k]]++] = s * 4 + k;
+    }
+    P.dptr.assign(P.n_active + 1, 0);
+    P.dlist.clear();
+    for (int n = 0; n < P.n_active; ++n) {
+        P.dlist.insert(P.dlist.end(), dl[n].begin(), dl[n].end());
+        P.dptr[n + 1] = (int)P.dlist.size();
+    }
+    // ---- receivers (visu_field, visualization.f90:156-181)
+    P.nrecv = prob.nrecv;
+    P.rnode.assign((size_t)4 * P.nrecv, 0);
+    P.rw.assign((size_t)4 * P.nrecv, 0.0);
+    P.rsoil.assign(P.nrecv, 0);
+    P.rxy.assign((size_t)2 * P.nrecv, 0.0);
+    for (int i = 0; i < P.nrecv; ++i) {
+        int e = prob.recv_elem[i] - 1;
+        if (e < 0 || e >= ne) { err = "receiver " + std::to_string(i + 1) + " element out of range"; return EXFEM_E_ARG; }
+        double px = prob.recv_xy[2 * i], py = prob.recv_xy[2 * i + 1];
+        const int *c = &corner_ref[(size_t)e * 4];
+        // shapeparams (formulation.f90:334-343) and shapefuncs (356-363)
+        double r = (px - xs[c[0]]) / (xs[c[2]] - xs[c[0]]);
+        double s = (py - ys[c[0]]) / (ys[c[2]] - ys[c[0]]);
+        r = 2.0 * r - 1.0; s = 2.0 * s - 1.0;
+        r = std::min(1.0, std::max(-1.0, r)); s = std::min(1.0, std::max(-1.0, s));
+        double inter[4] = {(1 - r) * (1 - s) / 4, (1 + r) * (1 - s) / 4, (1 + r) * (1 + s) / 4, (1 - r) * (1 + s) / 4};
+        for (int k = 0; k < 4; ++k) {
+            P.rnode[(size_t)4 * i + k] = P.node_of_ref[c[k]];
+            P.rw[(size_t)4 * i + k] = inter[k];
+        }
+        P.rsoil[i] = realunder(px, prob.wbox[0]) || realover(px, prob.wbox[1]) || realover(py, prob.wbox[2]);
+        P.rxy[2 * i] = px;
+        P.rxy[2 * i + 1] = py;
+    }
+    // ---- waves
+    P.waves.resize(P.R);
+    for (int r = 0; r < P.R; ++r) {
+        int rc = init_wave_const(prob.waves[r], prob.walpha, prob.wbeta, P.waves[r], err);
+        if (rc) { err = "rhs " + std::to_string(r) + ": " + err; return rc; }
+    }
+    return EXFEM_OK;
+}
+
+}  // namespace exfem

@@ -1,0 +1,84 @@
+// exfem_plan.h — host-side preparation of the device-resident model.
+//
+// Turns the reference-layout mesh/problem (include/exfem_gpu.h) into the
+// arrays the kernels read: a Morton-ordered internal numbering, per-element
+// Q4 operator coefficients, lumped mass/damping, the node-to-(element, corner)
+// gather lists that replace the element scatter of explicit.f90:141 and the
+// halo/anchor sums, the DRM slots and the receiver weights.  Pure C++ (no CUDA)
+// so it can be exercised without a GPU.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "exfem_gpu.h"
+
+namespace exfem {
+
+// Constants of one plane wave after initplanewaves (pwaves.f90:16-98).
+struct WaveConst {
+    int kind;
+    double alpha, beta, freq, fp;          // fp = freq*pi
+    double sine, cose, sinf, cosf;
+    double amp0, wa1, wb1;                 // incident (wa or wb), reflected P, reflected SV
+    double wui[6];                          // f_wui(2,3) column-major: (1,1),(2,1),(1,2),(2,2),(1,3),(2,3)
+    double t0;
+};
+
+int init_wave_const(const exfem_wave &w, double alpha, double beta, WaveConst &out, std::string &err);
+
+struct Plan {
+    int nn = 0, ne = 0, R = 1;
+    int n_active = 0;               // non-hanging nodes are internal [0, n_active)
+    int n_hang = 0;                 // hanging nodes are internal [n_active, nn)
+    double dt = 0, a1 = 0, a2 = 0, a3 = 0;
+    int nsteps = 0, io = 1, nsave = 1;
+    std::vector<int> ref_of_node;   // internal -> reference node (0-based)
+    std::vector<int> node_of_ref;   // reference -> internal
+    std::vector<int> ref_of_elem;   // internal -> reference element (0-based)
+    // elements (internal order)
+    std::vector<int> econn;         // 4 per element: internal node ids of the non-hanging corners
+    std::vector<double> ecoef;      // 4 per element: (lam+2mu)/4, lam/4, mu/4, (lam+3mu)/12
+    std::vector<float> ecoef32;     // same, FP32
+    std::vector<double> emulam;     // 2 per element: (mu, lambda) for calck in reference order
+    std::vector<double> emass;      // rho*(h/2)^2 per element (getmassof)
+    std::vector<int> edamp;         // per element: index into edampv or -1
+    std::vector<double> edampv;     // 8 per damped element (getdampingof)
+    // gather lists for active nodes; entry = ((elem*4 + corner) << 1) | half
+    std::vector<int> tptr, tlist;
+    std::vector<int> dptr, dlist;   // DRM: ((slot*4 + corner) << 1) | half
+    std::vector<double> mfull_ref;  // m_full in reference dof order (mass.bin)
+    std::vector<double> inv_mfull;  // 2 per active node (internal), 1/m_full
+    std::vector<double> mfull_int;  // 2 per active node (internal), m_full
+    // per node lumped terms (internal): M_n, C_n(x,y), D_n(x,y) = a1 M + a2 C, for the FP32 form
+    std::vector<double> nmass, ndamp;
+    // hanging entries (internal ids): h, a, b; hanging node of entry i is
+    // internal node n_active + i
+    std::vector<int> hang;
+    // DRM (seismic) elements
+    std::vector<int> s_elem, s_kind;
+    // receivers: the 4 non-hanging corners (internal ids) and their shape
+    // function weights (visu_field); a hanging corner is read as the average
+    // of its anchors
+    std::vector<int> rnode;
+    std::vector<double> rw;
+    std::vector<int> rsoil;
+    std::vector<double> rxy;
+    int nrecv = 0;
+    // waves
+    std::vector<WaveConst> waves;
+    double worigin[2] = {0, 0};
+    // per active node: hanging links (h, other anchor) in m_hanging order
+    std::vector<int> lptr, llist;   // llist entries: h internal, b internal (pairs)
+    // own incidences of every node (incl. hanging): elem*4+corner, sorted by
+    // reference element index (the order explicit.f90:129-142 adds them)
+    std::vector<int> ownptr, ownlist;
+    // own DRM incidences of every node: slot*4+corner in seismic order
+    std::vector<int> odptr, odlist;
+};
+
+// Build the plan.  Returns EXFEM_OK or an EXFEM_E_* code with err filled.
+int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &plan, std::string &err);
+
+}  // namespace exfem

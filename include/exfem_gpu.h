@@ -1,0 +1,190 @@
+/*
+ * exfem_gpu.h — C ABI of the GB300 (sm_103a) explicit time-stepping library.
+ *
+ * This is the drop-in boundary for the time loop of damian.par ("exfem"):
+ * the Fortran host keeps problem.in parsing, quadtree meshing and seismogram
+ * output and hands the finished model to this library instead of running
+ * init_explicit()/run_explicit() (explicit.f90:79-159) itself.
+ *
+ * Conventions follow the reference's own FFI (io.h:1-39, io_utils.f90:14-286):
+ * plain pointers and sizes, `extern "C"`, 1-based indices exactly as they sit
+ * in the Fortran arrays and in mesh.bin (io.cpp:333-367).  The caller owns every
+ * host array; the library copies what it needs to the device on create and only
+ * writes into caller-provided buffers (no malloc hand-off as in
+ * util_temps.m4:86-95).  Errors are negative status codes and a message string;
+ * the library never calls exit() (compare io.cpp:29-35, pwaves.f90:32-35, 87-89).
+ *
+ * Threading: one host thread per context; distinct contexts may be used from
+ * different threads, each runs on its own CUDA stream.
+ */
+#ifndef EXFEM_GPU_H
+#define EXFEM_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define EXFEM_OK               0
+#define EXFEM_E_ARG           -1   /* bad argument / inconsistent sizes          */
+#define EXFEM_E_MESH          -2   /* malformed mesh (non-hanging count != 4 ...) */
+#define EXFEM_E_NOMEM         -3   /* device or host allocation failed            */
+#define EXFEM_E_UNSUPPORTED   -4   /* grazing / post-critical wave, chained hanging */
+#define EXFEM_E_CUDA          -5   /* CUDA runtime error                          */
+#define EXFEM_E_NAN           -6   /* non-finite state detected by the watchdog   */
+#define EXFEM_E_TIMEOUT       -7   /* bounded device wait ran out                 */
+#define EXFEM_E_STATE         -8   /* call out of order (run before init ...)     */
+
+/* ---- wave kinds (m_prob, model.f90:692-696) ------------------------------ */
+#define EXFEM_WAVE_P   1           /* 'WAVEP ' */
+#define EXFEM_WAVE_SV  2           /* 'WAVESV' */
+
+/* ---- arithmetic forms ----------------------------------------------------- */
+#define EXFEM_FP64          0      /* plain FP64, same update as explicit.f90:126-152 */
+#define EXFEM_FP32_KAHAN    1      /* FP32 increment form, Kahan-compensated u      */
+
+/* ---- FP64 kernel variants ------------------------------------------------ */
+#define EXFEM_VARIANT_REFERENCE_ORDER 0  /* dense calck dgemv, element-order sums,
+                                            no contraction: the oracle's rounding */
+#define EXFEM_VARIANT_CLOSED_FORM     1  /* closed-form Q4 K.u with FMA (fewer
+                                            FP64 operations, rounding differs)  */
+
+/* ---- hanging-anchor reduction ---------------------------------------------- */
+#define EXFEM_HANG_HALF     0      /* r_a += r_h/2 (communicator.f90:1232 twin)     */
+#define EXFEM_HANG_LITERAL  1      /* text of model.f90:643-645 (oracle only)       */
+
+/* One plane wave = one right-hand side.  Mirrors the PROBLEM: parameters that
+ * init_wave() reads (model.f90:982-1001): m_wttoorigin = pparams(6),
+ * m_wangle = pparams(7), m_wamp = pparams(8), m_wfreq = pparams(9). */
+typedef struct exfem_wave {
+    int    kind;       /* EXFEM_WAVE_P or EXFEM_WAVE_SV                          */
+    double amp;        /* amplitude a (P) or b (SV)                              */
+    double angle;      /* incidence angle [rad]                                  */
+    double freq;       /* Ricker central frequency [Hz]                          */
+    double t0;         /* time to origin [s]                                      */
+} exfem_wave;
+
+/* The mesh as mesh.bin stores it (io.cpp:333-367; model.f90:51-61). */
+typedef struct exfem_mesh {
+    int nelems;
+    int nnodes;
+    const int           *eptr;      /* [nelems+1], 1-based CSR offsets (m_eptr)       */
+    const int           *eind;      /* [eptr[nelems]-1], 1-based node ids (m_eind)    */
+    const unsigned char *ediv;      /* [eptr[nelems]-1], 1 = hanging slot (m_ediv)    */
+    const double        *nodes;     /* [2*nnodes], (x, depth) pairs (m_nodes)          */
+    const int           *ematprop;  /* [nelems], 1-based material id (m_ematprop)     */
+} exfem_mesh;
+
+/* Everything problem_setup()/init_wave()/recalculate_deltat() leave in the
+ * model module (model.f90:21-101, 958-1106; communicator.f90:1629-1662). */
+typedef struct exfem_problem {
+    int           nmat;
+    const double *matconst;   /* [5*nmat] (mu, lambda, rho, vp, vs) per material   */
+    const int    *absorbing;  /* [nnodes] 0 none, 1 AB_ZDIR, 2 AB_XDIR            */
+    int           nhanging;
+    const int    *hanging;    /* [3*nhanging] (hanging, previous, next), 1-based   */
+    int           nseismic;
+    const int    *seismic;    /* [2*nseismic] (element, kind SE_*), 1-based        */
+    double        deltat;     /* m_deltat                                           */
+    int           nsteps;     /* m_nsteps                                           */
+    int           io_interval;/* io_interval (receivers are sampled on these steps) */
+    double        worigin[2]; /* m_worigin                                          */
+    double        wbox[3];    /* DRM box: left, right, top (model.f90:205-207)       */
+    double        walpha;     /* vp of the exterior material, m_wvelo(1)            */
+    double        wbeta;      /* vs of the exterior material, m_wvelo(2)            */
+    int           nrhs;
+    const exfem_wave *waves;  /* [nrhs]                                            */
+    int           nrecv;
+    const double *recv_xy;    /* [2*nrecv] receiver points (find_highest output)    */
+    const int    *recv_elem;  /* [nrecv] 1-based top element of each receiver       */
+} exfem_problem;
+
+typedef struct exfem_opts {
+    int precision;     /* EXFEM_FP64 or EXFEM_FP32_KAHAN                          */
+    int device;        /* CUDA device ordinal                                     */
+    int use_graph;     /* 1: replay the step as a captured CUDA graph             */
+    int graph_steps;   /* steps captured per graph (0 = library default)          */
+    int block_threads; /* node-kernel block size (0 = default / autotuned)        */
+    int rhs_per_thread;/* right-hand sides per thread in batched form (0 = auto)  */
+    int reorder;       /* 1: renumber nodes/elements in Morton order on device    */
+    int check_every;   /* non-finite watchdog period in steps (0 = off)           */
+    int variant;       /* FP64 kernels: EXFEM_VARIANT_REFERENCE_ORDER (default)
+                          or EXFEM_VARIANT_CLOSED_FORM                            */
+} exfem_opts;
+
+typedef struct exfem_ctx exfem_ctx;
+
+/* Fill *opts with defaults (FP64, device 0, graphs on, reorder on). */
+void exfem_gpu_default_opts(exfem_opts *opts);
+
+/* Build a device-resident model.  Replaces the state set up by init_model()
+ * for the solver (explicit.f90:16-70) — the host passes what it computed.
+ * Validates the mesh (elemallnhnodes' four non-hanging corners,
+ * model.f90:166-171), precomputes the per-node lumped mass/damping
+ * coefficients, the node-to-element gather lists and the DRM slots.
+ * Returns EXFEM_E_UNSUPPORTED for grazing/post-critical waves, where the
+ * reference would exit(1) (pwaves.f90:32-35, 87-89). */
+int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob,
+                     const exfem_opts *opts, exfem_ctx **out);
+
+/* init_explicit() (explicit.f90:79-109): zero state, assemble
+ * m_full = sum_e(a2*c_e + a1*m_e) with the hanging-anchor reduction.
+ * If mfull_out is non-NULL it receives m_full in the reference's dof order
+ * (2*nnodes doubles, the content of mass.bin, io.cpp:409-429). */
+int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out);
+
+/* run_explicit() (explicit.f90:111-159) for nsteps more steps (may be called
+ * repeatedly; the total may not exceed the problem's nsteps).  Receivers are
+ * sampled after every step with step % io_interval == 0 (save_step,
+ * io_utils.f90:390).  Asynchronous: returns after queueing the work. */
+int exfem_gpu_run(exfem_ctx *ctx, int nsteps);
+
+/* Wait for queued work; returns EXFEM_E_NAN if the watchdog tripped. */
+int exfem_gpu_sync(exfem_ctx *ctx);
+
+/* Current displacement e_u of right-hand side `rhs` (0-based) in the
+ * reference's dof order (2*nnodes doubles), as save_step would write it. */
+int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n);
+
+/* Receiver traces: out[rhs][save][recv][2] (x, depth components), the FIELD
+ * rows of sheet.txt (visualization.f90:307-354, io.cpp:862-876) including the
+ * free field outside the DRM box (visu_field, visualization.f90:156-181).
+ * *nsaved receives the number of stored samples per receiver. */
+int exfem_gpu_get_seismograms(exfem_ctx *ctx, double *out, size_t cap, int *nsaved);
+
+/* exfem_gpu_run() bracketed by CUDA events recorded on the context's own
+ * stream; waits for completion and returns the device time in *ms.  A
+ * measurement helper with no counterpart in the reference. */
+int exfem_gpu_run_timed(exfem_ctx *ctx, int nsteps, double *ms);
+
+/* Runs nsteps without graph capture, timing every launch with CUDA events on
+ * the context's stream.  ms_out[k] receives the average duration of kernel
+ * k, names_out[k] its name; returns the number of distinct kernels (at most
+ * cap).  A measurement helper with no counterpart in the reference. */
+int exfem_gpu_profile_kernels(exfem_ctx *ctx, int nsteps, double *ms_out, const char **names_out, int cap);
+
+/* Steps taken so far. */
+int exfem_gpu_steps_done(const exfem_ctx *ctx);
+
+/* Number of kernel launches the library queued so far (its own kernels). */
+long long exfem_gpu_launch_count(const exfem_ctx *ctx);
+
+/* Bytes of device memory held by the context. */
+size_t exfem_gpu_device_bytes(const exfem_ctx *ctx);
+
+/* Estimated device bytes a context for this mesh/problem/opts would hold
+ * (used for admission by HBM footprint).  No device work. */
+size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *prob,
+                                const exfem_opts *opts);
+
+/* Last error message of the context (or of the last failed create when ctx is NULL). */
+const char *exfem_gpu_last_error(const exfem_ctx *ctx);
+
+void exfem_gpu_destroy(exfem_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EXFEM_GPU_H */

@@ -1,0 +1,120 @@
+// probe.cu — test-only host build of the library's plan builder and of its
+// __host__ __device__ arithmetic, so the CPU suite can check both without a
+// GPU.  Compiled by tests/native_probe.py with nvcc into tests/native/_build.
+#include <cstring>
+#include <string>
+
+#include "exfem_device.cuh"
+#include "exfem_plan.h"
+
+using namespace exfem;
+
+namespace {
+std::string g_err;
+
+DevWave to_dev(const WaveConst &w) {
+    DevWave d;
+    d.kind = w.kind; d.alpha = w.alpha; d.beta = w.beta; d.fp = w.fp;
+    d.sine = w.sine; d.cose = w.cose; d.sinf = w.sinf; d.cosf = w.cosf;
+    d.amp0 = w.amp0; d.wa1 = w.wa1; d.wb1 = w.wb1;
+    for (int k = 0; k < 6; ++k) d.wui[k] = w.wui[k];
+    d.t0 = w.t0;
+    return d;
+}
+}  // namespace
+
+extern "C" {
+
+const char *probe_error(void) { return g_err.c_str(); }
+
+void probe_q4_ku(double A, double B, double C, double D, const double *ux, const double *uy, double *fx, double *fy) {
+    q4_ku<double>(A, B, C, D, ux, uy, fx, fy);
+}
+
+void probe_q4_ku_corner(double A, double B, double C, double D, const double *ux, const double *uy, int c,
+                        double *fx, double *fy) {
+    q4_ku_corner<double>(A, B, C, D, ux, uy, c, *fx, *fy);
+}
+
+void probe_q4_ku_f32(float A, float B, float C, float D, const float *ux, const float *uy, float *fx, float *fy) {
+    q4_ku<float>(A, B, C, D, ux, uy, fx, fy);
+}
+
+void probe_drm_forces(const double *k4, double mass, int kind, const double *u0, const double *a0, double *p) {
+    drm_forces(k4, mass, drm_mask(kind), u0, a0, p);
+}
+
+int probe_planewave(int kind, double amp, double alpha, double beta, double angle, double freq, double t, double x1,
+                    double x3, double *u6) {
+    exfem_wave w{kind, amp, angle, freq, 0.0};
+    WaveConst wc;
+    int rc = init_wave_const(w, alpha, beta, wc, g_err);
+    if (rc) return rc;
+    DevWave d = to_dev(wc);
+    double ux[3], uz[3];
+    planewave(d, t, x1, x3, ux, uz);
+    for (int c = 0; c < 3; ++c) { u6[2 * c] = ux[c]; u6[2 * c + 1] = uz[c]; }
+    return 0;
+}
+
+// The displacement-only path used by the receivers.
+int probe_planewave_u(int kind, double amp, double alpha, double beta, double angle, double freq, double t, double x1,
+                      double x3, double *u2) {
+    exfem_wave w{kind, amp, angle, freq, 0.0};
+    WaveConst wc;
+    int rc = init_wave_const(w, alpha, beta, wc, g_err);
+    if (rc) return rc;
+    DevWave d = to_dev(wc);
+    planewave_u(d, t, x1, x3, u2[0], u2[1]);
+    return 0;
+}
+
+void *probe_plan(const exfem_mesh *mesh, const exfem_problem *prob, int reorder) {
+    Plan *p = new Plan();
+    int rc = build_plan(*mesh, *prob, reorder != 0, *p, g_err);
+    if (rc) { delete p; return nullptr; }
+    return p;
+}
+
+void probe_plan_free(void *h) { delete static_cast<Plan *>(h); }
+
+// Sizes and copies of the plan arrays by name.
+long long probe_plan_size(void *h, const char *name) {
+    Plan &p = *static_cast<Plan *>(h);
+    std::string n(name);
+#define SZ(f) if (n == #f) return (long long)p.f.size();
+    SZ(ref_of_node) SZ(node_of_ref) SZ(ref_of_elem) SZ(econn) SZ(ecoef) SZ(emass) SZ(edamp) SZ(edampv)
+    SZ(tptr) SZ(tlist) SZ(dptr) SZ(dlist) SZ(mfull_ref) SZ(inv_mfull) SZ(nmass) SZ(ndamp) SZ(hang)
+    SZ(s_elem) SZ(s_kind) SZ(rnode) SZ(rw) SZ(rsoil) SZ(rxy) SZ(lptr) SZ(llist) SZ(ownptr) SZ(ownlist)
+#undef SZ
+    if (n == "scalars") return 8;
+    return -1;
+}
+
+int probe_plan_copy(void *h, const char *name, void *out) {
+    Plan &p = *static_cast<Plan *>(h);
+    std::string n(name);
+#define CP(f) if (n == #f) { if (!p.f.empty()) std::memcpy(out, p.f.data(), p.f.size() * sizeof(p.f[0])); return 0; }
+    CP(ref_of_node) CP(node_of_ref) CP(ref_of_elem) CP(econn) CP(ecoef) CP(emass) CP(edamp) CP(edampv)
+    CP(tptr) CP(tlist) CP(dptr) CP(dlist) CP(mfull_ref) CP(inv_mfull) CP(nmass) CP(ndamp) CP(hang)
+    CP(s_elem) CP(s_kind) CP(rnode) CP(rw) CP(rsoil) CP(rxy) CP(lptr) CP(llist) CP(ownptr) CP(ownlist)
+#undef CP
+    if (n == "scalars") {
+        double *d = static_cast<double *>(out);
+        d[0] = p.n_active; d[1] = p.n_hang; d[2] = p.a1; d[3] = p.a2; d[4] = p.a3; d[5] = p.dt; d[6] = p.nsave; d[7] = p.io;
+        return 0;
+    }
+    return -1;
+}
+
+// Free-field displacement+acceleration at a point for RHS r of a plan
+// (what k_drm evaluates).
+void probe_plan_wave(void *h, int r, double t, double x1, double x3, double *u6) {
+    Plan &p = *static_cast<Plan *>(h);
+    DevWave d = to_dev(p.waves[r]);
+    double ux[3], uz[3];
+    planewave(d, t - d.t0, x1, x3, ux, uz);
+    for (int c = 0; c < 3; ++c) { u6[2 * c] = ux[c]; u6[2 * c + 1] = uz[c]; }
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+"""Test helper: host build of the plan builder and device arithmetic (tests/native/probe.cu)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+PKG = os.path.join(REPO, "damian.par_gb300")
+sys.path.insert(0, PKG)
+from exfem.abi import ExfemError, Mesh, Problem  # noqa: E402
+
+SRC = [os.path.join(HERE, "native", "probe.cu"), os.path.join(PKG, "csrc", "exfem_plan.cpp")]
+DEPS = SRC + [os.path.join(PKG, "csrc", f) for f in ("exfem_plan.h", "exfem_device.cuh", "exfem_ctx.h")]
+OUT = os.path.join(HERE, "native", "_build", "libprobe.so")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    os.makedirs(os.path.dirname(OUT), exist_ok=True)
+    if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(os.path.getmtime(f) for f in DEPS):
+        tmp = OUT + ".tmp%d" % os.getpid()
+        cmd = [NVCC, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(REPO, "include"),
+               "-I", os.path.join(PKG, "csrc"), *SRC, "-o", tmp]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(res.stderr)
+        os.replace(tmp, OUT)
+    L = C.CDLL(OUT)
+    d = C.POINTER(C.c_double)
+    L.probe_error.restype = C.c_char_p
+    L.probe_q4_ku.argtypes = [C.c_double] * 4 + [d] * 4
+    L.probe_q4_ku_corner.argtypes = [C.c_double] * 4 + [d, d, C.c_int, d, d]
+    f = C.POINTER(C.c_float)
+    L.probe_q4_ku_f32.argtypes = [C.c_float] * 4 + [f] * 4
+    L.probe_drm_forces.argtypes = [d, C.c_double, C.c_int, d, d, d]
+    L.probe_planewave.restype = C.c_int
+    L.probe_planewave.argtypes = [C.c_int] + [C.c_double] * 8 + [d]
+    L.probe_planewave_u.restype = C.c_int
+    L.probe_planewave_u.argtypes = [C.c_int] + [C.c_double] * 8 + [d]
+    L.probe_plan.restype = C.c_void_p
+    L.probe_plan.argtypes = [C.POINTER(Mesh), C.POINTER(Problem), C.c_int]
+    L.probe_plan_free.argtypes = [C.c_void_p]
+    L.probe_plan_size.restype = C.c_longlong
+    L.probe_plan_size.argtypes = [C.c_void_p, C.c_char_p]
+    L.probe_plan_copy.restype = C.c_int
+    L.probe_plan_copy.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
+    L.probe_plan_wave.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, d]
+    _lib = L
+    return L
+
+
+def dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+INT_FIELDS = {"ref_of_node", "node_of_ref", "ref_of_elem", "econn", "edamp", "tptr", "tlist", "dptr", "dlist",
+              "hang", "s_elem", "s_kind", "rnode", "rsoil", "lptr", "llist", "ownptr", "ownlist"}
+
+
+class PlanView:
+    """All arrays of a host-built plan, as numpy arrays."""
+
+    def __init__(self, model, reorder=True):
+        L = lib()
+        self.h = L.probe_plan(C.byref(model.mesh), C.byref(model.problem), int(reorder))
+        if not self.h:
+            raise ExfemError(-1, L.probe_error().decode())
+        self.model = model
+
+    def __getattr__(self, name):
+        if name.startswith("_") or name in ("h", "model"):
+            raise AttributeError(name)
+        L = lib()
+        n = L.probe_plan_size(self.h, name.encode())
+        if n < 0:
+            raise AttributeError(name)
+        dtype = np.int32 if name in INT_FIELDS else np.float64
+        out = np.zeros(max(n, 1), dtype=dtype)
+        L.probe_plan_copy(self.h, name.encode(), out.ctypes.data_as(C.c_void_p))
+        out = out[:n]
+        self.__dict__[name] = out
+        return out
+
+    def wave(self, r, t, x1, x3):
+        out = np.zeros(6)
+        lib().probe_plan_wave(self.h, r, t, x1, x3, dp(out))
+        return out
+
+    def __del__(self):
+        h = self.__dict__.get("h")
+        if h:
+            lib().probe_plan_free(h)

@@ -1,0 +1,45 @@
+"""The C-ABI libraries load and export every symbol their headers declare
+(no compute call: these run without a GPU)."""
+import ctypes as C
+import os
+import re
+
+from exfem import _native
+from exfem.abi import EXFEM_E_ARG, Mesh, Opts, Problem
+
+INC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+
+
+def declared(header):
+    txt = open(os.path.join(INC, header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(exfem_\w+)\s*\(", txt)))
+
+
+def test_gpu_library_exports_header_symbols():
+    lib = C.CDLL(_native.GPU_LIB)
+    names = declared("exfem_gpu.h")
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_host_library_exports_header_symbols():
+    lib = C.CDLL(_native.HOST_LIB)
+    for n in declared("exfem_host.h"):
+        assert hasattr(lib, n), n
+
+
+def test_argument_errors_need_no_device():
+    from exfem.gpu import gpu_lib, default_opts
+    L = gpu_lib()
+    o = default_opts()
+    assert o.precision == 0 and o.use_graph == 1 and o.reorder == 1
+    h = C.c_void_p()
+    assert L.exfem_gpu_create(None, None, C.byref(o), C.byref(h)) == EXFEM_E_ARG
+    assert b"NULL" in L.exfem_gpu_last_error(None)
+    m = Mesh()
+    p = Problem()
+    assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(o), C.byref(h)) == EXFEM_E_ARG
+    bad = default_opts(block_threads=100)
+    assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
