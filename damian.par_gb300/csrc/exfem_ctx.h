@@ -107,3 +107,6 @@ int f32_launch_sample0(Ctx &c, int par);
 int f32_get_u(Ctx &c, int rhs, std::vector<double> &out_internal);
 
 }  // namespace exfem
+
+// The opaque handle of include/exfem_gpu.h.
+struct exfem_ctx : exfem::Ctx {};

@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "exfem_ctx.h"
 #include "exfem_device.cuh"
@@ -282,3 +284,92 @@ int f64_launch_hang(Ctx &c, double *unew, int mode) {
 }
 
 }  // namespace exfem
+
+// ---------------------------------------------------------------------------
+// Step without allocation (exfem_gpu_step_noalloc).
+//
+// Callers that keep the displacement state in device memory they manage
+// themselves and may not call cudaMalloc/cudaFree inside their time loop get
+// one FP64 step of their buffers here.  The per-step scratch — element forces,
+// DRM forces and the two step counters — lives in this file-scope array
+// instead of memory the library allocates.  Every device that loads the
+// library holds the array until the process exits.
+namespace exfem {
+namespace {
+
+constexpr size_t kNoallocScratchDoubles = EXFEM_NOALLOC_SCRATCH_DOUBLES;
+constexpr size_t kNoallocHeadDoubles = 32;   // counters, padded to 256 bytes
+
+__device__ __align__(256) double g_noalloc_scratch[kNoallocScratchDoubles];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current (host code only sees a stand-in for the symbol).
+std::mutex g_noalloc_mu;
+double *g_noalloc_addr[128] = {nullptr};
+
+// Resets the counters a step reads: device step = step - 1, flags, blocks.
+__global__ void k_noalloc_prep(int *counters, int step) {
+    counters[0] = step - 1;
+    counters[1] = 0;
+    counters[2] = 0;
+}
+
+}  // namespace
+
+}  // namespace exfem
+
+extern "C" int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const double *d_um,
+                                      double *d_unew) {
+    using namespace exfem;
+    if (!ctx || !d_u || !d_um || !d_unew) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    if (c.precision != EXFEM_FP64) { c.err = "exfem_gpu_step_noalloc needs an EXFEM_FP64 context"; return EXFEM_E_ARG; }
+    if (step < 1) { c.err = "step must be >= 1 (the time index i of explicit.f90:125)"; return EXFEM_E_ARG; }
+    const Plan &P = c.plan;
+    const size_t ns = P.s_elem.size();
+    const size_t ef_off = kNoallocHeadDoubles + ((ns * 16 * (size_t)P.R + 3) & ~(size_t)3);
+    const size_t need = ef_off + (size_t)P.ne * 8 * P.R;
+    if (need > kNoallocScratchDoubles) {
+        c.err = "exfem_gpu_step_noalloc: the model needs " + std::to_string(need) +
+                " doubles of scratch (8 per element and right-hand side, 16 per DRM element and right-hand side, "
+                "plus 32); the static limit is EXFEM_NOALLOC_SCRATCH_DOUBLES = " +
+                std::to_string(kNoallocScratchDoubles);
+        return EXFEM_E_ARG;
+    }
+    cudaError_t e = cudaSetDevice(c.device);
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    if (c.device < 0 || c.device >= 128) { c.err = "device ordinal out of range"; return EXFEM_E_ARG; }
+    double *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[c.device]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                c.err = std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e);
+                return EXFEM_E_CUDA;
+            }
+            g_noalloc_addr[c.device] = static_cast<double *>(p);
+        }
+        base = g_noalloc_addr[c.device];
+    }
+    DevModel m = c.dm;
+    int *counters = reinterpret_cast<int *>(base);
+    m.d_step = counters;
+    m.d_flag = counters + 1;
+    m.d_blocks = reinterpret_cast<unsigned *>(counters + 2);
+    m.fdrm = base + kNoallocHeadDoubles;
+    m.nrecv = 0;   // receivers stay with exfem_gpu_run
+    double *ef = base + ef_off;
+    const int T = 128;
+    k_noalloc_prep<<<1, 1, 0, c.stream>>>(counters, step);
+    if (m.ns > 0) k_drm_ref<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+    k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, d_u, d_um, ef);
+    k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, ef, d_unew);
+    int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);
+    k_hang_ref<<<nbh, T, 0, c.stream>>>(m, d_unew, nbh, 0);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    c.launches += 4 + (m.ns > 0 ? 1 : 0);
+    return EXFEM_OK;
+}

@@ -358,8 +358,6 @@ void mark(Ctx &c, const char *kernel) {
 }
 }  // namespace exfem
 
-struct exfem_ctx : Ctx {};
-
 extern "C" {
 
 void exfem_gpu_default_opts(exfem_opts *o) {

@@ -94,6 +94,7 @@ GPU_SYMBOLS = {
     "exfem_gpu_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "exfem_gpu_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                             C.POINTER(C.c_char_p), C.c_int]),
+    "exfem_gpu_step_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "exfem_gpu_steps_done": (C.c_int, [C.c_void_p]),
     "exfem_gpu_launch_count": (C.c_longlong, [C.c_void_p]),
     "exfem_gpu_device_bytes": (C.c_size_t, [C.c_void_p]),

@@ -165,6 +165,32 @@ int exfem_gpu_run_timed(exfem_ctx *ctx, int nsteps, double *ms);
  * cap).  A measurement helper with no counterpart in the reference. */
 int exfem_gpu_profile_kernels(exfem_ctx *ctx, int nsteps, double *ms_out, const char **names_out, int cap);
 
+/* Size of the static scratch array behind exfem_gpu_step_noalloc, in
+ * doubles (8 MiB; held by every device that loads the library). */
+#define EXFEM_NOALLOC_SCRATCH_DOUBLES 1048576
+
+/* One FP64 time step on buffers the caller owns, with no device allocation.
+ * No counterpart in the reference.
+ *
+ * For callers that keep the displacement state in device memory they manage
+ * themselves and may not call cudaMalloc or cudaFree while stepping: a host
+ * that captures its own time loop into a CUDA graph (allocation is not
+ * permitted while a stream is being captured) or a host whose own pool owns
+ * every device byte.  cudaFree would also synchronize the whole device.
+ *
+ * d_u, d_um: device arrays of u_i and u_{i-1}; d_unew receives u_{i+1}
+ * (2*nnodes*nrhs doubles each, the context's internal node order, the layout
+ * exfem_gpu_run keeps; d_unew may alias d_um).  `step` is the time index i+1
+ * whose forcing is applied (t = step*dt, explicit.f90:128).  Receivers are
+ * not sampled.  The element and DRM forces go through one static scratch
+ * array shared by every call: the model must fit
+ * 32 + 16*nseismic*nrhs + 8*nelems*nrhs <= EXFEM_NOALLOC_SCRATCH_DOUBLES
+ * (EXFEM_E_ARG otherwise), and calls that overlap on the GPU (two contexts,
+ * two streams) race on it.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  Queued on
+ * the context's stream; exfem_gpu_sync() waits for it. */
+int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const double *d_um, double *d_unew);
+
 /* Steps taken so far. */
 int exfem_gpu_steps_done(const exfem_ctx *ctx);
 
