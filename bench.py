@@ -33,7 +33,7 @@ for p in (HERE, os.path.join(HERE, "damian.par_gb300")):
 import numpy as np  # noqa: E402
 
 FORMS = {"fp64": 0, "fp32": 1}
-DEFAULT_WORKLOAD = ("canyon", "fp64")
+DEFAULT_WORKLOAD = ("valley_batched", "fp32")
 
 
 def dist_setup():
@@ -223,7 +223,16 @@ def run_ours(args, ws, rank, local, dist, torch):
     total = args.warmup + args.steps
     m = workloads.build(args.workload, scale=args.scale, steps=max(total, 8))
     R = m.problem.nrhs
-    s = Solver(m, precision=form, device=local)
+    tuned = {}
+    if args.block or args.rpt:
+        tuned = {k: v for k, v in (("block_threads", args.block), ("rhs_per_thread", args.rpt)) if v}
+    elif not fp64 and not args.no_extras:
+        from exfem import autotune
+        mt = workloads.build(args.workload, scale=args.scale, steps=24)
+        choice = autotune.tune(mt, steps=10, warmup=3, device=local)
+        tuned = {"block_threads": choice["block_threads"], "rhs_per_thread": choice["rhs_per_thread"]}
+        del mt
+    s = Solver(m, precision=form, device=local, **tuned)
     s.init_explicit()
     s.run(args.warmup)
     s.sync()
@@ -241,11 +250,19 @@ def run_ours(args, ws, rank, local, dist, torch):
     t_ms = allreduce_max(dist, torch, ms.value)
     s.close()
     value = ws * m.nelems * R * args.steps / (t_ms / 1000.0)
+    if args.no_extras:
+        if rank == 0:
+            print(json.dumps({"metric": "elem-steps/s", "value": value, "unit": "elem-steps*rhs/s", "n_gpus": ws,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+                              "config": {"workload": args.workload, "form": args.form, "scale": args.scale,
+                                         "elements": m.nelems, "rhs": R}, "tuned": tuned or None,
+                              "gpu_launches": launches, "clocks": clocks, "mode": "timed loop only"}))
+        return
 
     # per-kernel CUDA-event times on a fresh context (no graph, same stream)
     prof_steps = max(4, min(64, args.steps))
     mp = workloads.build(args.workload, scale=args.scale, steps=prof_steps + 2)
-    sp = Solver(mp, precision=form, device=local)
+    sp = Solver(mp, precision=form, device=local, **tuned)
     sp.init_explicit()
     sp.run(2)
     ms_arr = (C.c_double * 16)()
@@ -269,7 +286,7 @@ def run_ours(args, ws, rank, local, dist, torch):
     e2e_steps = args.steps
     me = workloads.build(args.workload, scale=args.scale, steps=e2e_steps)
     t0 = time.perf_counter()
-    se = Solver(me, precision=form, device=local)
+    se = Solver(me, precision=form, device=local, **tuned)
     se.init_explicit()
     se.run(e2e_steps)
     seis = se.seismograms()
@@ -278,6 +295,23 @@ def run_ours(args, ws, rank, local, dist, torch):
     e2e = {"value": ws * me.nelems * R * e2e_steps / t_e2e, "unit": "elem-steps*rhs/s",
            "h2d_bytes_per_step": input_bytes(me), "d2h_bytes_per_step": int(seis.nbytes),
            "note": "one request per bench step: create + init_explicit + %d steps + seismograms" % e2e_steps}
+
+    # the plain FP64 form on the same workload, for the FP32 / FP64 ratio
+    fp64_ref = None
+    if not fp64 and args.fp64_steps > 0:
+        mf = workloads.build(args.workload, scale=args.scale, steps=args.fp64_steps + 3)
+        sf = Solver(mf, device=local)
+        sf.init_explicit()
+        sf.run(3)
+        sf.sync()
+        msf = C.c_double(0)
+        rc = sf.lib.exfem_gpu_run_timed(sf.h, int(args.fp64_steps), C.byref(msf))
+        sf.close()
+        if rc == 0:
+            v64 = ws * mf.nelems * R * args.fp64_steps / (msf.value / 1000.0)
+            fp64_ref = {"value": v64, "ms_per_step": msf.value / args.fp64_steps, "steps": args.fp64_steps,
+                        "ratio_fp32_over_fp64": value / v64}
+        del mf
 
     if rank != 0:
         return
@@ -291,7 +325,8 @@ def run_ours(args, ws, rank, local, dist, torch):
                       "l2": "no flush: a bench step is one time step; the state of this workload is %.1f MB"
                             % ((2 * m.nnodes * R * (8 if fp64 else 4) * (2 if fp64 else 4)) / 1e6),
                       "parallelism": "replicas" if ws > 1 else "single"},
-           "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+           "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+           "tuned": tuned or None, "plain_fp64": fp64_ref}
     print(json.dumps(out))
 
 
@@ -304,6 +339,11 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD[0])
     ap.add_argument("--form", default=DEFAULT_WORKLOAD[1], choices=sorted(FORMS))
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="timed loop only (no autotune, kernel profile, e2e, CPU or FP64 legs): for ncu captures")
+    ap.add_argument("--block", type=int, default=0, help="force the step kernel's block size")
+    ap.add_argument("--rpt", type=int, default=0, help="force right-hand sides per thread")
+    ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

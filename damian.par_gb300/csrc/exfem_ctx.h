@@ -50,9 +50,9 @@ struct DevModel {
     const int *odptr, *odlist;     // own DRM incidences, all nodes, seismic order
     const int *lptr, *llist;       // anchor links (h, other anchor), m_hanging order
     // FP32 increment form
-    const float *ncoefA;           // per active node: (a1 M - a2 Cx, a1 M - a2 Cy) pairs
-    const float *nD;               // per node: D = a1 M + a2 C (x, y)
-    const float *inv_mfull32;      // 2 per active node
+    const float *ncoef4;           // per active node: 1/m_full (x, y), a1 M - a2 C (x, y)
+    const float *hcoef4;           // per hanging entry: a1 M - a2 C (x, y), a1 M + a2 C (x, y)
+    float *fdrm32;                 // ns * 8 * R DRM forces (FP64 math, stored FP32)
     // mutable state
     double *fdrm;            // ns * 16 * R DRM forces (stiffness part, mass part)
     double *seis;            // R * nsave * nrecv * 2

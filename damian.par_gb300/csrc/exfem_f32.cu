@@ -1,12 +1,428 @@
 // exfem_f32.cu — FP32 increment form with Kahan-compensated displacements.
+//
+// The central-difference update of explicit.f90:135-148,
+//   (a1 M + a2 C) u+ = f - K u + 2 a1 M u - a1 M u- + a2 C u-,
+// rewritten for the increment D = u - u- (exact algebra):
+//   D+ = (f - K u + (a1 M - a2 C) D) / m_full,   u+ = u + D+,
+// so FP32 carries the small increment instead of the difference of two
+// large displacements.  u is kept as an FP32 value plus a Kahan compensation
+// term (true u = u_hi - comp).  Anchors of hanging nodes add half of each
+// hanging node's term (sum_reactanchors, halving form), which in the increment
+// form carries the extra D_h (u_h - u_a) = D_h (u_b - u_a)/2 because the
+// hanging node's mass acts on its own displacement.  Templates, masses,
+// dashpots, hanging weights and dt stay FP64 on the host and are rounded once.
+//
+// One step is three kernels:
+//   k_drm32    DRM effective forces in FP64, stored FP32
+//   k_step32   per (non-hanging node, group of right-hand sides): gather the
+//              closed-form Q4 forces of its elements from u_hi, the DRM terms,
+//              the lumped terms, update D and u (fused; no element buffer)
+//   k_hang32   hanging nodes = anchor averages; receivers in FP64
+// State layout: value (node n, dof d, rhs r) at (n*2 + d)*R + r, so a warp
+// reads R contiguous floats per (node, dof) and one set of mesh metadata
+// serves every right-hand side.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "exfem_ctx.h"
+#include "exfem_device.cuh"
 
 namespace exfem {
 
-int f32_alloc(Ctx &c) { c.err = "FP32 form not built yet"; return EXFEM_E_UNSUPPORTED; }
-int f32_init(Ctx &c) { c.err = "FP32 form not built yet"; return EXFEM_E_UNSUPPORTED; }
-int f32_launch_step(Ctx &c, int) { c.err = "FP32 form not built yet"; return EXFEM_E_UNSUPPORTED; }
-int f32_launch_sample0(Ctx &c, int) { c.err = "FP32 form not built yet"; return EXFEM_E_UNSUPPORTED; }
-int f32_get_u(Ctx &c, int, std::vector<double> &) { c.err = "FP32 form not built yet"; return EXFEM_E_UNSUPPORTED; }
+namespace {
+
+#define CK(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            c.err = std::string(#call) + ": " + cudaGetErrorString(e_);           \
+            return EXFEM_E_CUDA;                                                  \
+        }                                                                         \
+    } while (0)
+
+template <int N>
+struct Vec;
+template <>
+struct Vec<1> {
+    using T = float;
+    __device__ static void load(const float *p, float *v) { v[0] = __ldg(p); }
+    __device__ static void load_cg(const float *p, float *v) { v[0] = *p; }
+    __device__ static void store(float *p, const float *v) { *p = v[0]; }
+};
+template <>
+struct Vec<2> {
+    __device__ static void load(const float *p, float *v) {
+        float2 a = __ldg(reinterpret_cast<const float2 *>(p));
+        v[0] = a.x; v[1] = a.y;
+    }
+    __device__ static void load_cg(const float *p, float *v) {
+        float2 a = *reinterpret_cast<const float2 *>(p);
+        v[0] = a.x; v[1] = a.y;
+    }
+    __device__ static void store(float *p, const float *v) { *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]); }
+};
+template <>
+struct Vec<4> {
+    __device__ static void load(const float *p, float *v) {
+        float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+    __device__ static void load_cg(const float *p, float *v) {
+        float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+    __device__ static void store(float *p, const float *v) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+
+__device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
+
+// DRM forces (model.f90:745-800) in FP64, stored FP32.
+__global__ void k_drm32(DevModel m) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.ns * m.R) return;
+    int s = (int)(t / m.R), r = (int)(t % m.R);
+    int step = read_step(m) + 1;
+    const DevWave w = m.waves[r];
+    double outt = (double)step * m.dt - w.t0;
+    int ie = m.s_elem[s];
+    double u0[8], a0[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int x = m.econn[4 * ie + k];
+        double ux[3], uz[3];
+        planewave(w, outt, m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, ux, uz);
+        u0[2 * k] = ux[0]; u0[2 * k + 1] = uz[0];
+        a0[2 * k] = ux[2]; a0[2 * k + 1] = uz[2];
+    }
+    double kc[4] = {m.ecoef[4 * ie], m.ecoef[4 * ie + 1], m.ecoef[4 * ie + 2], m.ecoef[4 * ie + 3]};
+    double p[8];
+    drm_forces(kc, m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) m.fdrm32[((size_t)s * 8 + k) * m.R + r] = (float)p[k];
+}
+
+// The fused step for one non-hanging node and RPT right-hand sides.
+template <int RPT>
+__global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
+                                                float *__restrict__ uc, float *__restrict__ du) {
+    const int G = m.R / RPT;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.n_active * G) return;
+    const int n = (int)(t / G);
+    const int r0 = (int)(t % G) * RPT;
+    const size_t R = m.R;
+    float ax[RPT], ay[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) { ax[j] = 0.f; ay[j] = 0.f; }
+    // DRM terms (hanging corners at half weight in their anchors)
+    for (int q = m.dptr[n]; q < m.dptr[n + 1]; ++q) {
+        int ent = __ldg(m.dlist + q);
+        float w = (ent & 1) ? 0.5f : 1.0f;
+        int sc = ent >> 1;
+        size_t b = ((size_t)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
+        float fx[RPT], fy[RPT];
+        Vec<RPT>::load_cg(m.fdrm32 + b, fx);
+        Vec<RPT>::load_cg(m.fdrm32 + b + R, fy);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
+    }
+    // element terms: -K_e u_e at this node's corner (and its hanging nodes' at 1/2)
+    const int4 *econn4 = reinterpret_cast<const int4 *>(m.econn);
+    const float4 *coef4 = reinterpret_cast<const float4 *>(m.ecoef32);
+    for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
+        int ent = __ldg(m.tlist + q);
+        float w = (ent & 1) ? 0.5f : 1.0f;
+        int ec = ent >> 1;
+        int e = ec >> 2, c = ec & 3;
+        int4 cn = __ldg(econn4 + e);
+        float4 k = __ldg(coef4 + e);
+        const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
+        float ux[4][RPT], uy[4][RPT];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            size_t b = ((size_t)cc[v] * 2) * R + r0;
+            Vec<RPT>::load(uh + b, ux[v]);
+            Vec<RPT>::load(uh + b + R, uy[v]);
+        }
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
+            float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
+            float fx, fy;
+            q4_ku_corner<float>(k.x, k.y, k.z, k.w, vx, vy, c, fx, fy);
+            ax[j] -= w * fx;
+            ay[j] -= w * fy;
+        }
+    }
+    // lumped mass and dashpot terms: (a1 M - a2 C) D
+    const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
+    const size_t bn = ((size_t)n * 2) * R + r0;
+    float dx[RPT], dy[RPT], unx[RPT], uny[RPT];
+    Vec<RPT>::load_cg(du + bn, dx);
+    Vec<RPT>::load_cg(du + bn + R, dy);
+    Vec<RPT>::load(uh + bn, unx);
+    Vec<RPT>::load(uh + bn + R, uny);
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
+    // hanging nodes this node anchors: 1/2 [ (a1 M_h - a2 C_h) D_h + D_h,mass (u_b - u_n)/2 ]
+    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
+        int h = __ldg(m.llist + 2 * q), b = __ldg(m.llist + 2 * q + 1);
+        float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
+        size_t bh = ((size_t)h * 2) * R + r0, bb = ((size_t)b * 2) * R + r0;
+        float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
+        Vec<RPT>::load_cg(du + bh, hx);
+        Vec<RPT>::load_cg(du + bh + R, hy);
+        Vec<RPT>::load(uh + bb, ubx);
+        Vec<RPT>::load(uh + bb + R, uby);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j])));
+            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j])));
+        }
+    }
+    // D+ = r / m_full; u+ = u + D+ with Kahan compensation
+    float cx[RPT], cy[RPT];
+    Vec<RPT>::load_cg(uc + bn, cx);
+    Vec<RPT>::load_cg(uc + bn + R, cy);
+    float nx_[RPT], ny_[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        float dnx = ax[j] * nc.x, dny = ay[j] * nc.y;
+        dx[j] = dnx;
+        dy[j] = dny;
+        float yx = dnx - cx[j], yy = dny - cy[j];
+        float tx = unx[j] + yx, ty = uny[j] + yy;
+        cx[j] = (tx - unx[j]) - yx;
+        cy[j] = (ty - uny[j]) - yy;
+        nx_[j] = tx;
+        ny_[j] = ty;
+    }
+    Vec<RPT>::store(du + bn, dx);
+    Vec<RPT>::store(du + bn + R, dy);
+    Vec<RPT>::store(uc + bn, cx);
+    Vec<RPT>::store(uc + bn + R, cy);
+    Vec<RPT>::store(uhn + bn, nx_);
+    Vec<RPT>::store(uhn + bn + R, ny_);
+}
+
+// u of one node in FP64 (u_hi - comp); hanging corners read as anchor averages.
+__device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, const float *uc, int node, int r,
+                                         double &vx, double &vy) {
+    const size_t R = m.R;
+    auto val = [&](int x, int d) {
+        size_t i = ((size_t)x * 2 + d) * R + r;
+        return (double)uh[i] - (double)uc[i];
+    };
+    if (node < m.n_active) {
+        vx = val(node, 0);
+        vy = val(node, 1);
+    } else {
+        int i = node - m.n_active;
+        int a = m.hang[3 * i + 1], b = m.hang[3 * i + 2];
+        vx = (val(a, 0) + val(b, 0)) / 2.0;
+        vy = (val(a, 1) + val(b, 1)) / 2.0;
+    }
+}
+
+// Hanging nodes (anchor averages of u_hi, comp and D) and receivers.
+__global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ uhn, float *__restrict__ uc,
+                                                float *__restrict__ du, int nb_hang, int mode) {
+    int step = (mode == 1) ? 0 : read_step(m) + 1;
+    const size_t R = m.R;
+    if ((int)blockIdx.x < nb_hang) {
+        long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (mode == 0 && t < (long long)m.n_hang * m.R) {
+            int i = (int)(t / m.R), r = (int)(t % m.R);
+            int h = m.hang[3 * i], a = m.hang[3 * i + 1], b = m.hang[3 * i + 2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                size_t ih = ((size_t)h * 2 + d) * R + r, ia = ((size_t)a * 2 + d) * R + r,
+                       ib = ((size_t)b * 2 + d) * R + r;
+                uhn[ih] = 0.5f * (uhn[ia] + uhn[ib]);
+                uc[ih] = 0.5f * (uc[ia] + uc[ib]);
+                du[ih] = 0.5f * (du[ia] + du[ib]);
+            }
+        }
+    } else if (step % m.io == 0) {
+        long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
+        if (t < (long long)m.nrecv * m.R) {
+            int i = (int)(t % m.nrecv), r = (int)(t / m.nrecv);
+            int slot = step / m.io;
+            double fx = 0.0, fy = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                double vx, vy;
+                load_u32(m, uhn, uc, m.rnode[4 * i + k], r, vx, vy);
+                double w = m.rw[4 * i + k];
+                fx += w * vx;
+                fy += w * vy;
+            }
+            if (m.rsoil[i]) {
+                const DevWave wv = m.waves[r];
+                double time = m.dt * (double)slot * (double)m.io;
+                double ddx, ddz;
+                planewave_u(wv, time - wv.t0, m.rxy[2 * i] - m.worigin_x, m.rxy[2 * i + 1] - m.worigin_y, ddx, ddz);
+                fx += ddx;
+                fy += ddz;
+            }
+            size_t o = (((size_t)r * m.nsave + slot) * m.nrecv + i) * 2;
+            m.seis[o] = fx;
+            m.seis[o + 1] = fy;
+            if (!isfinite(fx) || !isfinite(fy)) atomicOr(m.d_flag, 1);
+        }
+    }
+    if (mode == 0) {   // the last block advances the device step counter
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            unsigned prev = atomicAdd(m.d_blocks, 1u);
+            if (prev == gridDim.x - 1) {
+                *m.d_step = *m.d_step + 1;
+                *m.d_blocks = 0u;
+                __threadfence();
+            }
+        }
+    }
+}
+
+inline int nblocks(long long work, int threads) { return (int)std::max<long long>(1, (work + threads - 1) / threads); }
+
+template <typename T>
+int upload32(Ctx &c, const std::vector<T> &v, const T **dst) {
+    if (v.empty()) { *dst = nullptr; return EXFEM_OK; }
+    void *p = nullptr;
+    CK(cudaMalloc(&p, v.size() * sizeof(T)));
+    c.allocs.push_back(p);
+    c.bytes += v.size() * sizeof(T);
+    CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    *dst = static_cast<const T *>(p);
+    return EXFEM_OK;
+}
+
+template <typename T>
+int alloc32(Ctx &c, size_t n, T **dst) {
+    void *p = nullptr;
+    if (n == 0) n = 1;
+    CK(cudaMalloc(&p, n * sizeof(T)));
+    c.allocs.push_back(p);
+    c.bytes += n * sizeof(T);
+    *dst = static_cast<T *>(p);
+    return EXFEM_OK;
+}
+
+}  // namespace
+
+// Right-hand sides per thread: the largest of 4, 2, 1 dividing R (or the
+// requested one when it divides R).
+static int pick_rpt(const Ctx &c) {
+    int R = c.plan.R;
+    int want = c.opts.rhs_per_thread;
+    if (want == 1 || want == 2 || want == 4) return (R % want == 0) ? want : 1;
+    if (R % 4 == 0 && R >= 32) return 4;
+    if (R % 2 == 0 && R >= 16) return 2;
+    return 1;
+}
+
+int f32_alloc(Ctx &c) {
+    const Plan &P = c.plan;
+    DevModel &m = c.dm;
+    // per active node: 1/m_full (x, y), a1 M - a2 C (x, y)
+    std::vector<float> nc((size_t)4 * P.n_active);
+    for (int n = 0; n < P.n_active; ++n) {
+        nc[4 * (size_t)n] = (float)P.inv_mfull[2 * (size_t)n];
+        nc[4 * (size_t)n + 1] = (float)P.inv_mfull[2 * (size_t)n + 1];
+        nc[4 * (size_t)n + 2] = (float)(P.a1 * P.nmass[n] - P.a2 * P.ndamp[2 * (size_t)n]);
+        nc[4 * (size_t)n + 3] = (float)(P.a1 * P.nmass[n] - P.a2 * P.ndamp[2 * (size_t)n + 1]);
+    }
+    std::vector<float> hc((size_t)4 * std::max(P.n_hang, 1), 0.f);
+    for (int i = 0; i < P.n_hang; ++i) {
+        int h = P.hang[3 * (size_t)i];
+        hc[4 * (size_t)i] = (float)(P.a1 * P.nmass[h] - P.a2 * P.ndamp[2 * (size_t)h]);
+        hc[4 * (size_t)i + 1] = (float)(P.a1 * P.nmass[h] - P.a2 * P.ndamp[2 * (size_t)h + 1]);
+        hc[4 * (size_t)i + 2] = (float)(P.a1 * P.nmass[h] + P.a2 * P.ndamp[2 * (size_t)h]);
+        hc[4 * (size_t)i + 3] = (float)(P.a1 * P.nmass[h] + P.a2 * P.ndamp[2 * (size_t)h + 1]);
+    }
+    int rc;
+    if ((rc = upload32(c, nc, &m.ncoef4))) return rc;
+    if ((rc = upload32(c, hc, &m.hcoef4))) return rc;
+    if ((rc = upload32(c, P.ecoef32, &m.ecoef32))) return rc;
+    if ((rc = alloc32(c, (size_t)std::max(m.ns, 1) * 8 * P.R, &m.fdrm32))) return rc;
+    size_t nst = (size_t)P.nn * 2 * P.R;
+    if ((rc = alloc32(c, nst, &c.uhi[0]))) return rc;
+    if ((rc = alloc32(c, nst, &c.uhi[1]))) return rc;
+    if ((rc = alloc32(c, nst, &c.ucomp))) return rc;
+    if ((rc = alloc32(c, nst, &c.udel[0]))) return rc;
+    c.rhs_per_thread = pick_rpt(c);
+    if (c.opts.block_threads <= 0) c.block_threads = 256;
+    return EXFEM_OK;
+}
+
+int f32_init(Ctx &c) {
+    size_t nst = (size_t)c.plan.nn * 2 * c.plan.R * sizeof(float);
+    CK(cudaMemsetAsync(c.uhi[0], 0, nst, c.stream));
+    CK(cudaMemsetAsync(c.uhi[1], 0, nst, c.stream));
+    CK(cudaMemsetAsync(c.ucomp, 0, nst, c.stream));
+    CK(cudaMemsetAsync(c.udel[0], 0, nst, c.stream));
+    return EXFEM_OK;
+}
+
+int f32_launch_step(Ctx &c, int par) {
+    DevModel &m = c.dm;
+    float *uh = c.uhi[par], *uhn = c.uhi[par ^ 1];
+    if (m.ns > 0) {
+        k_drm32<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+        c.launches++;
+        mark(c, "k_drm32");
+    }
+    const int T = c.block_threads;
+    const int rpt = c.rhs_per_thread;
+    long long work = (long long)m.n_active * (m.R / rpt);
+    switch (rpt) {
+        case 4: k_step32<4><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0]); break;
+        case 2: k_step32<2><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0]); break;
+        default: k_step32<1><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0]); break;
+    }
+    c.launches++;
+    mark(c, "k_step32");
+    const int TH = 256;
+    int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + TH - 1) / TH);
+    int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
+    k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uhn, c.ucomp, c.udel[0], nbh, 0);
+    c.launches++;
+    mark(c, "k_hang32");
+    CK(cudaGetLastError());
+    return EXFEM_OK;
+}
+
+int f32_launch_sample0(Ctx &c, int par) {
+    DevModel &m = c.dm;
+    const int TH = 256;
+    int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
+    if (nbr > 0) {
+        k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.ucomp, c.udel[0], 0, 1);
+        c.launches++;
+    }
+    CK(cudaGetLastError());
+    return EXFEM_OK;
+}
+
+int f32_get_u(Ctx &c, int rhs, std::vector<double> &out) {
+    const Plan &P = c.plan;
+    size_t nst = (size_t)P.nn * 2 * P.R;
+    std::vector<float> hi(nst), co(nst);
+    CK(cudaMemcpy(hi.data(), c.uhi[c.parity], nst * sizeof(float), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(co.data(), c.ucomp, nst * sizeof(float), cudaMemcpyDeviceToHost));
+    out.resize((size_t)P.nn * 2);
+    for (int i = 0; i < P.nn; ++i)
+        for (int d = 0; d < 2; ++d) {
+            size_t k = ((size_t)i * 2 + d) * P.R + rhs;
+            out[2 * (size_t)i + d] = (double)hi[k] - (double)co[k];
+        }
+    return EXFEM_OK;
+}
 
 }  // namespace exfem

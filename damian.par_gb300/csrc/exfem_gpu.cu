@@ -386,8 +386,9 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
         g_create_err = "unknown kernel variant";
         return EXFEM_E_ARG;
     }
-    if (o.block_threads < 0 || o.block_threads > 1024 || (o.block_threads % 32) != 0) {
-        g_create_err = "block_threads must be a multiple of 32 in [0, 1024]";
+    const int max_bt = o.precision == EXFEM_FP64 ? 256 : 512;   // the kernels' __launch_bounds__
+    if (o.block_threads < 0 || o.block_threads > max_bt || (o.block_threads % 32) != 0) {
+        g_create_err = "block_threads must be a multiple of 32 in [0, " + std::to_string(max_bt) + "]";
         return EXFEM_E_ARG;
     }
     exfem_ctx *c = nullptr;

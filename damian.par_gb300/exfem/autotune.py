@@ -1,0 +1,60 @@
+"""Autotuner for the FP32 step kernel's launch shape.
+
+Tries (block size, right-hand sides per thread) on the real model: each
+candidate gets its own context, a few warm-up steps and a CUDA-event-timed
+burst on the library's stream; the fastest shape wins.  Results are cached
+per (elements, nodes, rhs) in-process.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from .abi import EXFEM_FP32_KAHAN, ExfemError
+from .gpu import Solver
+
+_cache: dict = {}
+
+
+def candidates(R):
+    rpts = [r for r in (1, 2, 4) if R % r == 0]
+    return [(bt, r) for r in rpts for bt in (128, 256, 512)]
+
+
+def tune(model, steps=12, warmup=3, device=0, verbose=False):
+    key = (model.nelems, model.nnodes, model.problem.nrhs)
+    if key in _cache:
+        return _cache[key]
+    R = model.problem.nrhs
+    best = None
+    results = []
+    need = warmup + steps
+    if model.problem.nsteps < need:
+        raise ExfemError(-1, "autotune needs %d steps in the model" % need)
+    for bt, rpt in candidates(R):
+        try:
+            s = Solver(model, precision=EXFEM_FP32_KAHAN, device=device, block_threads=bt, rhs_per_thread=rpt,
+                       use_graph=0)
+        except ExfemError:
+            continue
+        try:
+            s.init_explicit()
+            s.run(warmup)
+            s.sync()
+            ms = C.c_double(0)
+            rc = s.lib.exfem_gpu_run_timed(s.h, steps, C.byref(ms))
+        except ExfemError:
+            rc = -1
+        finally:
+            s.close()
+        if rc != 0:
+            continue
+        results.append((ms.value / steps, bt, rpt))
+        if best is None or ms.value < best[0]:
+            best = (ms.value, bt, rpt)
+    if verbose:
+        for r in sorted(results):
+            print("autotune: %.4f ms/step block %d rhs/thread %d" % r)
+    choice = {"block_threads": best[1], "rhs_per_thread": best[2], "ms_per_step": best[0] / steps,
+              "tried": [{"ms_per_step": a, "block_threads": b, "rhs_per_thread": c} for a, b, c in sorted(results)]}
+    _cache[key] = choice
+    return choice

@@ -119,3 +119,100 @@ def emulate_fp64(model, nsteps, rhs=0, reorder=True):
     u_ref = np.zeros((nn, 2))
     u_ref[P.ref_of_node] = u
     return {"seis": seis, "u": u_ref.ravel(), "mfull": P.mfull_ref}
+
+
+def emulate_fp32_kahan(model, nsteps, rhs=0):
+    """float32 twin of k_drm32/k_step32/k_hang32 (increment form, Kahan u)."""
+    P = npb.PlanView(model)
+    sc = P.scalars
+    na, nh = int(sc[0]), int(sc[1])
+    a1, a2, dt = sc[2], sc[3], sc[5]
+    io = int(sc[7])
+    nn = model.nnodes
+    f32 = np.float32
+    econn = P.econn.reshape(-1, 4)
+    ecoef = P.ecoef.reshape(-1, 4)
+    k32 = ecoef.astype(f32)
+    emass = P.emass
+    nodes = model.nodes()[P.ref_of_node]
+    worigin = np.array(model.problem.worigin[:])
+    s_elem, s_kind = P.s_elem, P.s_kind
+    ns = s_elem.size
+    tptr, tlist = P.tptr, P.tlist
+    dptr, dlist = P.dptr, P.dlist
+    t_node = np.repeat(np.arange(na), np.diff(tptr))
+    t_w = np.where(tlist & 1, f32(0.5), f32(1.0)).astype(f32)
+    t_e = (tlist >> 1) >> 2
+    t_c = (tlist >> 1) & 3
+    d_node = np.repeat(np.arange(na), np.diff(dptr))
+    d_w = np.where(dlist & 1, 0.5, 1.0).astype(f32)
+    d_s = (dlist >> 1) >> 2
+    d_c = (dlist >> 1) & 3
+    inv_m = P.inv_mfull.reshape(-1, 2).astype(f32)
+    nmass, ndamp = P.nmass, P.ndamp.reshape(-1, 2)
+    B = (a1 * nmass[:, None] - a2 * ndamp).astype(f32)
+    D = (a1 * nmass[:, None] + a2 * ndamp).astype(f32)
+    hang = P.hang.reshape(-1, 3)
+    lptr, llist = P.lptr, P.llist.reshape(-1, 2)
+    l_node = np.repeat(np.arange(na), np.diff(lptr))
+    rnode, rw = P.rnode.reshape(-1, 4), P.rw.reshape(-1, 4)
+    rsoil, rxy = P.rsoil, P.rxy.reshape(-1, 2)
+    nsave = nsteps // io + 1
+    seis = np.zeros((nsave, rsoil.size, 2))
+    L = npb.lib()
+    uh = np.zeros((nn, 2), f32)
+    uc = np.zeros((nn, 2), f32)
+    du = np.zeros((nn, 2), f32)
+
+    def sample(slot):
+        time = dt * slot * io
+        u = uh.astype(np.float64) - uc.astype(np.float64)
+        if nh:
+            u[hang[:, 0]] = (u[hang[:, 1]] + u[hang[:, 2]]) / 2
+        f = np.einsum("rk,rkc->rc", rw, u[rnode])
+        for i in np.nonzero(rsoil)[0]:
+            f[i] += P.wave(rhs, time, rxy[i, 0] - worigin[0], rxy[i, 1] - worigin[1])[0:2]
+        seis[slot] = f
+
+    sample(0)
+    for step in range(1, nsteps + 1):
+        t = step * dt
+        fdrm = np.zeros((max(ns, 1), 8), f32)
+        for s in range(ns):
+            ie = s_elem[s]
+            u0, a0 = np.zeros(8), np.zeros(8)
+            for k in range(4):
+                x = econn[ie, k]
+                w = P.wave(rhs, t, nodes[x, 0] - worigin[0], nodes[x, 1] - worigin[1])
+                u0[2 * k:2 * k + 2] = w[0:2]
+                a0[2 * k:2 * k + 2] = w[4:6]
+            p = np.zeros(8)
+            kc = np.ascontiguousarray(ecoef[ie])
+            L.probe_drm_forces(npb.dp(kc), float(emass[ie]), int(s_kind[s]), npb.dp(u0), npb.dp(a0), npb.dp(p))
+            fdrm[s] = p.astype(f32)
+        fx, fy = q4_ku(k32, uh[econn, 0], uh[econn, 1])
+        acc = np.zeros((na, 2), f32)
+        if dlist.size:
+            np.add.at(acc, d_node, d_w[:, None] * np.stack([fdrm[d_s, 2 * d_c], fdrm[d_s, 2 * d_c + 1]], axis=1))
+        np.add.at(acc, t_node, -t_w[:, None] * np.stack([fx[t_e, t_c], fy[t_e, t_c]], axis=1))
+        acc += B[:na] * du[:na]
+        if llist.size:
+            h, b = llist[:, 0], llist[:, 1]
+            term = f32(0.5) * (B[h] * du[h] + D[h] * (f32(0.5) * (uh[b] - uh[l_node])))
+            np.add.at(acc, l_node, term)
+        dn = (acc * inv_m).astype(f32)
+        du[:na] = dn
+        y = (dn - uc[:na]).astype(f32)
+        tt = (uh[:na] + y).astype(f32)
+        uc[:na] = ((tt - uh[:na]).astype(f32) - y).astype(f32)
+        uh_new = uh.copy()
+        uh_new[:na] = tt
+        if nh:
+            a_, b_ = hang[:, 1], hang[:, 2]
+            uh_new[hang[:, 0]] = f32(0.5) * (uh_new[a_] + uh_new[b_])
+            uc[hang[:, 0]] = f32(0.5) * (uc[a_] + uc[b_])
+            du[hang[:, 0]] = f32(0.5) * (du[a_] + du[b_])
+        uh = uh_new
+        if step % io == 0:
+            sample(step // io)
+    return {"seis": seis}

@@ -41,5 +41,5 @@ def test_argument_errors_need_no_device():
     m = Mesh()
     p = Problem()
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(o), C.byref(h)) == EXFEM_E_ARG
-    bad = default_opts(block_threads=100)
+    bad = default_opts(block_threads=512)   # FP64 kernels take at most 256
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG

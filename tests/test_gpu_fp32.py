@@ -1,0 +1,108 @@
+"""FP32 increment form with Kahan-compensated displacements, batched over
+right-hand sides, against the FP64 oracle and the FP64 GPU form.
+
+Tolerance: <= 1e-4 relative L2 per receiver seismogram (both components over
+time); peak-amplitude error is checked at the same level."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from exfem import decks, workloads
+from exfem.abi import EXFEM_E_NAN, EXFEM_FP32_KAHAN, ExfemError
+from exfem.gpu import Solver
+from exfem.model import Model
+from oracle import oracle
+from util import peak_rel, per_receiver_rel
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+NT = os.cpu_count() or 8
+
+
+def run32(m, steps=None, **opts):
+    with Solver(m, precision=EXFEM_FP32_KAHAN, **opts) as s:
+        s.init_explicit()
+        s.run(steps)
+        s.sync()
+        return s.seismograms(), [s.u(r) for r in range(s.nrhs)]
+
+
+def test_rectangle_fp32_vs_oracle():
+    m = workloads.build("homogeneous_rectangle", scale=0.25, steps=600)
+    o = oracle.run(m, nthreads=NT)
+    g, _ = run32(m)
+    assert per_receiver_rel(g[0], o["seis"]).max() <= TOL
+    assert peak_rel(g[0], o["seis"]).max() <= TOL
+
+
+def test_canyon_fp32_every_rhs_vs_oracle():
+    m = workloads.build("canyon", scale=0.15, steps=900, save_every=2, refine_band=20)
+    g, _ = run32(m)
+    for r in range(m.problem.nrhs):
+        o = oracle.run(m, rhs=r, nthreads=NT)
+        assert np.abs(o["seis"]).max() > 0.1
+        assert per_receiver_rel(g[r], o["seis"]).max() <= TOL, r
+
+
+@pytest.mark.parametrize("rpt", [1, 2, 4])
+def test_batched_valley_rhs_match_oracle_for_every_tile(rpt):
+    m = workloads.build("valley_batched", scale=0.1, steps=500, save_every=5)
+    assert m.problem.nrhs == 64
+    g, _ = run32(m, rhs_per_thread=rpt, block_threads=128 * rpt)
+    for r in (0, 21, 40, 63):
+        o = oracle.run(m, rhs=r, nthreads=NT)
+        err = per_receiver_rel(g[r], o["seis"])
+        assert err.max() <= TOL, (r, err.max())
+
+
+def test_result_is_the_same_alone_and_in_the_batch():
+    batch = workloads.build("valley_batched", scale=0.1, steps=300, save_every=3)
+    gb, _ = run32(batch)
+    waves = batch.waves()
+    for r in (5, 37):
+        w = waves[r]
+        kind = "WAVEP" if w.kind == 1 else "WAVESV"
+        alone = Model(decks.valley(scale=0.1, steps=300, rhs=[(kind, w.angle, w.amp, w.freq)]), nsteps=300,
+                      io_interval=3)
+        assert abs(alone.waves()[0].t0 - w.t0) < 1e-12
+        ga, _ = run32(alone)
+        assert per_receiver_rel(ga[0], gb[r]).max() <= 1e-6
+
+
+def test_fp32_vs_fp64_gpu_on_full_canyon():
+    """Full-size canyon (~1.9e5 elements, hanging nodes), 4000 steps (2.5 s,
+    past every wave's arrival): the FP32 form against the FP64 form, per
+    receiver and right-hand side."""
+    m = workloads.build("canyon", steps=4000)
+    g32, _ = run32(m)
+    with Solver(m) as s:
+        s.init_explicit()
+        s.run()
+        s.sync()
+        g64 = s.seismograms()
+    for r in range(m.problem.nrhs):
+        assert np.abs(g64[r]).max() > 0.1
+        assert per_receiver_rel(g32[r], g64[r]).max() <= TOL, r
+
+
+def test_diverging_run_is_reported():
+    """dt five times over the stability limit: the watchdog turns the blow-up
+    into EXFEM_E_NAN at sync instead of silent garbage."""
+    d = decks.homogeneous_rectangle(scale=0.125, steps=400).replace("CONTROL:\n10.0 2.0", "CONTROL:\n10.0 0.4")
+    m = Model(d)   # the deck's TIME now gives 80 steps of the larger dt
+    with Solver(m, precision=EXFEM_FP32_KAHAN) as s:
+        s.init_explicit()
+        s.run()
+        with pytest.raises(ExfemError) as e:
+            s.sync()
+        assert e.value.code == EXFEM_E_NAN
+
+
+def test_autotuner_picks_a_working_shape():
+    from exfem import autotune
+    m = workloads.build("valley_batched", scale=0.1, steps=40)
+    choice = autotune.tune(m, steps=8, warmup=2)
+    assert choice["rhs_per_thread"] in (1, 2, 4) and choice["block_threads"] in (128, 256, 512)
+    assert len(choice["tried"]) >= 6
