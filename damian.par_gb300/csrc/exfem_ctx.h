@@ -50,8 +50,8 @@ struct DevModel {
     const int *odptr, *odlist;     // own DRM incidences, all nodes, seismic order
     const int *lptr, *llist;       // anchor links (h, other anchor), m_hanging order
     // FP32 increment form
-    const float *ncoef4;           // per active node: 1/m_full (x, y), a1 M - a2 C (x, y)
-    const float *hcoef4;           // per hanging entry: a1 M - a2 C (x, y), a1 M + a2 C (x, y)
+    const float *ncoef4;           // per active node: 1/m_full (x, y), -2 a2 C (x, y)
+    const float *hcoef4;           // per hanging entry: -2 a2 C (x, y), a1 M + a2 C (x, y)
     float *fdrm32;                 // ns * 8 * R DRM forces (FP64 math, stored FP32)
     // mutable state
     double *fdrm;            // ns * 16 * R DRM forces (stiffness part, mass part)
@@ -73,10 +73,12 @@ struct Ctx {
     // FP64 state: u[2] ping-pong + element forces
     double *u64[2] = {nullptr, nullptr};
     double *ef64 = nullptr;
-    // FP32 state: hi[2] ping-pong, compensation, increment
+    // FP32 state: u_hi[2] ping-pong and the increment D in FP32, each with a
+    // bf16 Kahan compensation (stored as raw 16-bit words)
     float *uhi[2] = {nullptr, nullptr};
-    float *ucomp = nullptr;
+    unsigned short *ucomp = nullptr;
     float *udel[2] = {nullptr, nullptr};
+    unsigned short *dcomp = nullptr;
     int parity = 0;          // index of the current u buffer
     int steps_done = 0;
     bool inited = false;
@@ -105,6 +107,8 @@ int f32_init(Ctx &c);
 int f32_launch_step(Ctx &c, int par);
 int f32_launch_sample0(Ctx &c, int par);
 int f32_get_u(Ctx &c, int rhs, std::vector<double> &out_internal);
+// bf16 <-> float on the host (round to nearest even), for tests and read-back.
+float bf16_to_float(unsigned short h);
 
 }  // namespace exfem
 

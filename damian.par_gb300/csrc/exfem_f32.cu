@@ -1,30 +1,37 @@
-// exfem_f32.cu — FP32 increment form with Kahan-compensated displacements.
+// exfem_f32.cu — FP32 increment form with Kahan-compensated state.
 //
 // The central-difference update of explicit.f90:135-148,
 //   (a1 M + a2 C) u+ = f - K u + 2 a1 M u - a1 M u- + a2 C u-,
 // rewritten for the increment D = u - u- (exact algebra):
-//   D+ = (f - K u + (a1 M - a2 C) D) / m_full,   u+ = u + D+,
-// so FP32 carries the small increment instead of the difference of two
-// large displacements.  u is kept as an FP32 value plus a Kahan compensation
-// term (true u = u_hi - comp).  Anchors of hanging nodes add half of each
-// hanging node's term (sum_reactanchors, halving form), which in the increment
-// form carries the extra D_h (u_h - u_a) = D_h (u_b - u_a)/2 because the
-// hanging node's mass acts on its own displacement.  Templates, masses,
-// dashpots, hanging weights and dt stay FP64 on the host and are rounded once.
+//   D+ = D + delta,  delta = (f - K u - 2 a2 C D) / m_full,   u+ = u + D+.
+// delta holds only the small physical terms, so FP32 keeps its relative
+// precision; D and u are each accumulated with a Kahan compensation term
+// (true value = hi - comp).  Without the compensation on D its rounding
+// random-walks (about sqrt(steps) * 2^-24 of the peak); the compensations are
+// stored as bf16 (FP32's exponent range, 8 extra bits), so the state stays at
+// 12 bytes per dof: u_hi 4 + u_comp 2 + D 4 + D_comp 2.
+// Anchors of hanging nodes add half of each hanging node's term
+// (sum_reactanchors, halving form); in the increment form that carries
+// D_h ((u_b - u_a)/2 + (D_h - D_a)) because the hanging node's mass acts on
+// its own displacement and increment.  Templates, masses, dashpots, hanging
+// weights and dt stay FP64 on the host and are rounded once.
 //
 // One step is three kernels:
 //   k_drm32    DRM effective forces in FP64, stored FP32
 //   k_step32   per (non-hanging node, group of right-hand sides): gather the
 //              closed-form Q4 forces of its elements from u_hi, the DRM terms,
-//              the lumped terms, update D and u (fused; no element buffer)
+//              the dashpot and anchor terms, update D and u (fused; no
+//              element buffer)
 //   k_hang32   hanging nodes = anchor averages; receivers in FP64
 // State layout: value (node n, dof d, rhs r) at (n*2 + d)*R + r, so a warp
-// reads R contiguous floats per (node, dof) and one set of mesh metadata
+// reads R contiguous values per (node, dof) and one set of mesh metadata
 // serves every right-hand side.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "exfem_ctx.h"
@@ -79,6 +86,52 @@ struct Vec<4> {
     }
 };
 
+// RPT bf16 values (raw 16-bit words) <-> float.
+template <int N>
+struct Half;
+template <>
+struct Half<1> {
+    __device__ static void load(const unsigned short *p, float *v) {
+        v[0] = __bfloat162float(__ushort_as_bfloat16(*p));
+    }
+    __device__ static void store(unsigned short *p, const float *v) {
+        *p = __bfloat16_as_ushort(__float2bfloat16_rn(v[0]));
+    }
+};
+template <>
+struct Half<2> {
+    __device__ static void load(const unsigned short *p, float *v) {
+        unsigned w = *reinterpret_cast<const unsigned *>(p);
+        v[0] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(w & 0xffffu)));
+        v[1] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(w >> 16)));
+    }
+    __device__ static void store(unsigned short *p, const float *v) {
+        unsigned lo = __bfloat16_as_ushort(__float2bfloat16_rn(v[0]));
+        unsigned hi = __bfloat16_as_ushort(__float2bfloat16_rn(v[1]));
+        *reinterpret_cast<unsigned *>(p) = lo | (hi << 16);
+    }
+};
+template <>
+struct Half<4> {
+    __device__ static void load(const unsigned short *p, float *v) {
+        uint2 w = *reinterpret_cast<const uint2 *>(p);
+        v[0] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(w.x & 0xffffu)));
+        v[1] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(w.x >> 16)));
+        v[2] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(w.y & 0xffffu)));
+        v[3] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(w.y >> 16)));
+    }
+    __device__ static void store(unsigned short *p, const float *v) {
+        unsigned a = __bfloat16_as_ushort(__float2bfloat16_rn(v[0]));
+        unsigned b = __bfloat16_as_ushort(__float2bfloat16_rn(v[1]));
+        unsigned c = __bfloat16_as_ushort(__float2bfloat16_rn(v[2]));
+        unsigned d = __bfloat16_as_ushort(__float2bfloat16_rn(v[3]));
+        *reinterpret_cast<uint2 *>(p) = make_uint2(a | (b << 16), c | (d << 16));
+    }
+};
+
+__device__ __forceinline__ float bf2f(unsigned short h) { return __bfloat162float(__ushort_as_bfloat16(h)); }
+__device__ __forceinline__ unsigned short f2bf(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+
 __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
 
 // DRM forces (model.f90:745-800) in FP64, stored FP32.
@@ -109,7 +162,8 @@ __global__ void k_drm32(DevModel m) {
 // The fused step for one non-hanging node and RPT right-hand sides.
 template <int RPT>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
-                                                float *__restrict__ uc, float *__restrict__ du) {
+                                                unsigned short *__restrict__ uc, float *__restrict__ dh,
+                                                unsigned short *__restrict__ dc) {
     const int G = m.R / RPT;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m.n_active * G) return;
@@ -159,64 +213,77 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
             ay[j] -= w * fy;
         }
     }
-    // lumped mass and dashpot terms: (a1 M - a2 C) D
+    // dashpot term -2 a2 C D (zero away from the absorbing boundary)
     const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
     const size_t bn = ((size_t)n * 2) * R + r0;
-    float dx[RPT], dy[RPT], unx[RPT], uny[RPT];
-    Vec<RPT>::load_cg(du + bn, dx);
-    Vec<RPT>::load_cg(du + bn + R, dy);
+    float dx[RPT], dy[RPT];
+    Vec<RPT>::load_cg(dh + bn, dx);
+    Vec<RPT>::load_cg(dh + bn + R, dy);
+    if (nc.z != 0.f || nc.w != 0.f) {
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
+    }
+    float unx[RPT], uny[RPT];
     Vec<RPT>::load(uh + bn, unx);
     Vec<RPT>::load(uh + bn + R, uny);
-#pragma unroll
-    for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
-    // hanging nodes this node anchors: 1/2 [ (a1 M_h - a2 C_h) D_h + D_h,mass (u_b - u_n)/2 ]
+    // hanging nodes this node anchors:
+    //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_b - u_n)/2 + (D_h - D_n)) ]
+    // (D_b - D_n = 2 (D_h - D_n); D_h is read instead of D_b because the
+    // other anchor's thread rewrites D_b in place during this kernel, while
+    // D_h changes only in k_hang32)
     for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
         int h = __ldg(m.llist + 2 * q), b = __ldg(m.llist + 2 * q + 1);
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
         size_t bh = ((size_t)h * 2) * R + r0, bb = ((size_t)b * 2) * R + r0;
         float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
-        Vec<RPT>::load_cg(du + bh, hx);
-        Vec<RPT>::load_cg(du + bh + R, hy);
+        Vec<RPT>::load_cg(dh + bh, hx);
+        Vec<RPT>::load_cg(dh + bh + R, hy);
         Vec<RPT>::load(uh + bb, ubx);
         Vec<RPT>::load(uh + bb + R, uby);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
-            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j])));
-            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j])));
+            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j]) + (hx[j] - dx[j])));
+            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j]) + (hy[j] - dy[j])));
         }
     }
-    // D+ = r / m_full; u+ = u + D+ with Kahan compensation
-    float cx[RPT], cy[RPT];
-    Vec<RPT>::load_cg(uc + bn, cx);
-    Vec<RPT>::load_cg(uc + bn + R, cy);
-    float nx_[RPT], ny_[RPT];
+    // delta = r / m_full; D+ = D + delta and u+ = u + D+, both Kahan-compensated
+    float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
+    Half<RPT>::load(dc + bn, dcx);
+    Half<RPT>::load(dc + bn + R, dcy);
+    Half<RPT>::load(uc + bn, ucx);
+    Half<RPT>::load(uc + bn + R, ucy);
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
-        float dnx = ax[j] * nc.x, dny = ay[j] * nc.y;
-        dx[j] = dnx;
-        dy[j] = dny;
-        float yx = dnx - cx[j], yy = dny - cy[j];
-        float tx = unx[j] + yx, ty = uny[j] + yy;
-        cx[j] = (tx - unx[j]) - yx;
-        cy[j] = (ty - uny[j]) - yy;
-        nx_[j] = tx;
-        ny_[j] = ty;
+        float yx = ax[j] * nc.x - dcx[j], yy = ay[j] * nc.y - dcy[j];
+        float tx = dx[j] + yx, ty = dy[j] + yy;
+        dcx[j] = (tx - dx[j]) - yx;
+        dcy[j] = (ty - dy[j]) - yy;
+        dx[j] = tx;
+        dy[j] = ty;
+        float vx = tx - ucx[j], vy = ty - ucy[j];
+        float sx = unx[j] + vx, sy = uny[j] + vy;
+        ucx[j] = (sx - unx[j]) - vx;
+        ucy[j] = (sy - uny[j]) - vy;
+        ox[j] = sx;
+        oy[j] = sy;
     }
-    Vec<RPT>::store(du + bn, dx);
-    Vec<RPT>::store(du + bn + R, dy);
-    Vec<RPT>::store(uc + bn, cx);
-    Vec<RPT>::store(uc + bn + R, cy);
-    Vec<RPT>::store(uhn + bn, nx_);
-    Vec<RPT>::store(uhn + bn + R, ny_);
+    Vec<RPT>::store(dh + bn, dx);
+    Vec<RPT>::store(dh + bn + R, dy);
+    Half<RPT>::store(dc + bn, dcx);
+    Half<RPT>::store(dc + bn + R, dcy);
+    Half<RPT>::store(uc + bn, ucx);
+    Half<RPT>::store(uc + bn + R, ucy);
+    Vec<RPT>::store(uhn + bn, ox);
+    Vec<RPT>::store(uhn + bn + R, oy);
 }
 
 // u of one node in FP64 (u_hi - comp); hanging corners read as anchor averages.
-__device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, const float *uc, int node, int r,
-                                         double &vx, double &vy) {
+__device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, const unsigned short *uc, int node,
+                                         int r, double &vx, double &vy) {
     const size_t R = m.R;
     auto val = [&](int x, int d) {
         size_t i = ((size_t)x * 2 + d) * R + r;
-        return (double)uh[i] - (double)uc[i];
+        return (double)uh[i] - (double)bf2f(uc[i]);
     };
     if (node < m.n_active) {
         vx = val(node, 0);
@@ -230,8 +297,9 @@ __device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, con
 }
 
 // Hanging nodes (anchor averages of u_hi, comp and D) and receivers.
-__global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ uhn, float *__restrict__ uc,
-                                                float *__restrict__ du, int nb_hang, int mode) {
+__global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ uhn,
+                                                unsigned short *__restrict__ uc, float *__restrict__ dh,
+                                                unsigned short *__restrict__ dc, int nb_hang, int mode) {
     int step = (mode == 1) ? 0 : read_step(m) + 1;
     const size_t R = m.R;
     if ((int)blockIdx.x < nb_hang) {
@@ -244,8 +312,9 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ 
                 size_t ih = ((size_t)h * 2 + d) * R + r, ia = ((size_t)a * 2 + d) * R + r,
                        ib = ((size_t)b * 2 + d) * R + r;
                 uhn[ih] = 0.5f * (uhn[ia] + uhn[ib]);
-                uc[ih] = 0.5f * (uc[ia] + uc[ib]);
-                du[ih] = 0.5f * (du[ia] + du[ib]);
+                uc[ih] = f2bf(0.5f * (bf2f(uc[ia]) + bf2f(uc[ib])));
+                dh[ih] = 0.5f * (dh[ia] + dh[ib]);
+                dc[ih] = f2bf(0.5f * (bf2f(dc[ia]) + bf2f(dc[ib])));
             }
         }
     } else if (step % m.io == 0) {
@@ -330,19 +399,19 @@ static int pick_rpt(const Ctx &c) {
 int f32_alloc(Ctx &c) {
     const Plan &P = c.plan;
     DevModel &m = c.dm;
-    // per active node: 1/m_full (x, y), a1 M - a2 C (x, y)
+    // per active node: 1/m_full (x, y), -2 a2 C (x, y)
     std::vector<float> nc((size_t)4 * P.n_active);
     for (int n = 0; n < P.n_active; ++n) {
         nc[4 * (size_t)n] = (float)P.inv_mfull[2 * (size_t)n];
         nc[4 * (size_t)n + 1] = (float)P.inv_mfull[2 * (size_t)n + 1];
-        nc[4 * (size_t)n + 2] = (float)(P.a1 * P.nmass[n] - P.a2 * P.ndamp[2 * (size_t)n]);
-        nc[4 * (size_t)n + 3] = (float)(P.a1 * P.nmass[n] - P.a2 * P.ndamp[2 * (size_t)n + 1]);
+        nc[4 * (size_t)n + 2] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)n]);
+        nc[4 * (size_t)n + 3] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)n + 1]);
     }
     std::vector<float> hc((size_t)4 * std::max(P.n_hang, 1), 0.f);
     for (int i = 0; i < P.n_hang; ++i) {
         int h = P.hang[3 * (size_t)i];
-        hc[4 * (size_t)i] = (float)(P.a1 * P.nmass[h] - P.a2 * P.ndamp[2 * (size_t)h]);
-        hc[4 * (size_t)i + 1] = (float)(P.a1 * P.nmass[h] - P.a2 * P.ndamp[2 * (size_t)h + 1]);
+        hc[4 * (size_t)i] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)h]);
+        hc[4 * (size_t)i + 1] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)h + 1]);
         hc[4 * (size_t)i + 2] = (float)(P.a1 * P.nmass[h] + P.a2 * P.ndamp[2 * (size_t)h]);
         hc[4 * (size_t)i + 3] = (float)(P.a1 * P.nmass[h] + P.a2 * P.ndamp[2 * (size_t)h + 1]);
     }
@@ -356,17 +425,19 @@ int f32_alloc(Ctx &c) {
     if ((rc = alloc32(c, nst, &c.uhi[1]))) return rc;
     if ((rc = alloc32(c, nst, &c.ucomp))) return rc;
     if ((rc = alloc32(c, nst, &c.udel[0]))) return rc;
+    if ((rc = alloc32(c, nst, &c.dcomp))) return rc;
     c.rhs_per_thread = pick_rpt(c);
     if (c.opts.block_threads <= 0) c.block_threads = 256;
     return EXFEM_OK;
 }
 
 int f32_init(Ctx &c) {
-    size_t nst = (size_t)c.plan.nn * 2 * c.plan.R * sizeof(float);
-    CK(cudaMemsetAsync(c.uhi[0], 0, nst, c.stream));
-    CK(cudaMemsetAsync(c.uhi[1], 0, nst, c.stream));
-    CK(cudaMemsetAsync(c.ucomp, 0, nst, c.stream));
-    CK(cudaMemsetAsync(c.udel[0], 0, nst, c.stream));
+    size_t nst = (size_t)c.plan.nn * 2 * c.plan.R;
+    CK(cudaMemsetAsync(c.uhi[0], 0, nst * sizeof(float), c.stream));
+    CK(cudaMemsetAsync(c.uhi[1], 0, nst * sizeof(float), c.stream));
+    CK(cudaMemsetAsync(c.ucomp, 0, nst * sizeof(unsigned short), c.stream));
+    CK(cudaMemsetAsync(c.udel[0], 0, nst * sizeof(float), c.stream));
+    CK(cudaMemsetAsync(c.dcomp, 0, nst * sizeof(unsigned short), c.stream));
     return EXFEM_OK;
 }
 
@@ -382,16 +453,16 @@ int f32_launch_step(Ctx &c, int par) {
     const int rpt = c.rhs_per_thread;
     long long work = (long long)m.n_active * (m.R / rpt);
     switch (rpt) {
-        case 4: k_step32<4><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0]); break;
-        case 2: k_step32<2><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0]); break;
-        default: k_step32<1><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0]); break;
+        case 4: k_step32<4><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        case 2: k_step32<2><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        default: k_step32<1><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
     }
     c.launches++;
     mark(c, "k_step32");
     const int TH = 256;
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + TH - 1) / TH);
     int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
-    k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uhn, c.ucomp, c.udel[0], nbh, 0);
+    k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0);
     c.launches++;
     mark(c, "k_hang32");
     CK(cudaGetLastError());
@@ -403,7 +474,7 @@ int f32_launch_sample0(Ctx &c, int par) {
     const int TH = 256;
     int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
     if (nbr > 0) {
-        k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.ucomp, c.udel[0], 0, 1);
+        k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.ucomp, c.udel[0], c.dcomp, 0, 1);
         c.launches++;
     }
     CK(cudaGetLastError());
@@ -413,16 +484,24 @@ int f32_launch_sample0(Ctx &c, int par) {
 int f32_get_u(Ctx &c, int rhs, std::vector<double> &out) {
     const Plan &P = c.plan;
     size_t nst = (size_t)P.nn * 2 * P.R;
-    std::vector<float> hi(nst), co(nst);
+    std::vector<float> hi(nst);
+    std::vector<unsigned short> co(nst);
     CK(cudaMemcpy(hi.data(), c.uhi[c.parity], nst * sizeof(float), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(co.data(), c.ucomp, nst * sizeof(float), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(co.data(), c.ucomp, nst * sizeof(unsigned short), cudaMemcpyDeviceToHost));
     out.resize((size_t)P.nn * 2);
     for (int i = 0; i < P.nn; ++i)
         for (int d = 0; d < 2; ++d) {
             size_t k = ((size_t)i * 2 + d) * P.R + rhs;
-            out[2 * (size_t)i + d] = (double)hi[k] - (double)co[k];
+            out[2 * (size_t)i + d] = (double)hi[k] - (double)bf16_to_float(co[k]);
         }
     return EXFEM_OK;
+}
+
+float bf16_to_float(unsigned short h) {
+    unsigned w = (unsigned)h << 16;
+    float f;
+    std::memcpy(&f, &w, sizeof(f));
+    return f;
 }
 
 }  // namespace exfem

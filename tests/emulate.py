@@ -121,8 +121,17 @@ def emulate_fp64(model, nsteps, rhs=0, reorder=True):
     return {"seis": seis, "u": u_ref.ravel(), "mfull": P.mfull_ref}
 
 
-def emulate_fp32_kahan(model, nsteps, rhs=0):
-    """float32 twin of k_drm32/k_step32/k_hang32 (increment form, Kahan u)."""
+def bf16(x):
+    """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32)
+    r = ((b + np.uint32(0x7FFF) + ((b >> np.uint32(16)) & np.uint32(1))) & np.uint32(0xFFFF0000)).astype(np.uint32)
+    return r.view(np.float32)
+
+
+def emulate_fp32(model, nsteps, rhs=0, comp="bf16"):
+    """float32 twin of k_drm32/k_step32/k_hang32: delta = (f - K u - 2 a2 C D
+    + anchor terms) / m_full, D+ = D + delta and u+ = u + D+, both Kahan
+    compensated, the compensations stored as `comp` ("bf16" or "f32")."""
     P = npb.PlanView(model)
     sc = P.scalars
     na, nh = int(sc[0]), int(sc[1])
@@ -130,6 +139,7 @@ def emulate_fp32_kahan(model, nsteps, rhs=0):
     io = int(sc[7])
     nn = model.nnodes
     f32 = np.float32
+    rnd = bf16 if comp == "bf16" else (lambda v: np.asarray(v, f32))
     econn = P.econn.reshape(-1, 4)
     ecoef = P.ecoef.reshape(-1, 4)
     k32 = ecoef.astype(f32)
@@ -138,31 +148,25 @@ def emulate_fp32_kahan(model, nsteps, rhs=0):
     worigin = np.array(model.problem.worigin[:])
     s_elem, s_kind = P.s_elem, P.s_kind
     ns = s_elem.size
-    tptr, tlist = P.tptr, P.tlist
-    dptr, dlist = P.dptr, P.dlist
+    tptr, tlist, dptr, dlist = P.tptr, P.tlist, P.dptr, P.dlist
     t_node = np.repeat(np.arange(na), np.diff(tptr))
-    t_w = np.where(tlist & 1, f32(0.5), f32(1.0)).astype(f32)
-    t_e = (tlist >> 1) >> 2
-    t_c = (tlist >> 1) & 3
+    t_w = np.where(tlist & 1, 0.5, 1.0).astype(f32)
+    t_e, t_c = (tlist >> 1) >> 2, (tlist >> 1) & 3
     d_node = np.repeat(np.arange(na), np.diff(dptr))
     d_w = np.where(dlist & 1, 0.5, 1.0).astype(f32)
-    d_s = (dlist >> 1) >> 2
-    d_c = (dlist >> 1) & 3
+    d_s, d_c = (dlist >> 1) >> 2, (dlist >> 1) & 3
     inv_m = P.inv_mfull.reshape(-1, 2).astype(f32)
     nmass, ndamp = P.nmass, P.ndamp.reshape(-1, 2)
-    B = (a1 * nmass[:, None] - a2 * ndamp).astype(f32)
+    E = (-2.0 * a2 * ndamp).astype(f32)
     D = (a1 * nmass[:, None] + a2 * ndamp).astype(f32)
     hang = P.hang.reshape(-1, 3)
     lptr, llist = P.lptr, P.llist.reshape(-1, 2)
     l_node = np.repeat(np.arange(na), np.diff(lptr))
     rnode, rw = P.rnode.reshape(-1, 4), P.rw.reshape(-1, 4)
     rsoil, rxy = P.rsoil, P.rxy.reshape(-1, 2)
-    nsave = nsteps // io + 1
-    seis = np.zeros((nsave, rsoil.size, 2))
+    seis = np.zeros((nsteps // io + 1, rsoil.size, 2))
     L = npb.lib()
-    uh = np.zeros((nn, 2), f32)
-    uc = np.zeros((nn, 2), f32)
-    du = np.zeros((nn, 2), f32)
+    uh, uc, dh, dc = (np.zeros((nn, 2), f32) for _ in range(4))
 
     def sample(slot):
         time = dt * slot * io
@@ -195,24 +199,28 @@ def emulate_fp32_kahan(model, nsteps, rhs=0):
         if dlist.size:
             np.add.at(acc, d_node, d_w[:, None] * np.stack([fdrm[d_s, 2 * d_c], fdrm[d_s, 2 * d_c + 1]], axis=1))
         np.add.at(acc, t_node, -t_w[:, None] * np.stack([fx[t_e, t_c], fy[t_e, t_c]], axis=1))
-        acc += B[:na] * du[:na]
+        acc += E[:na] * dh[:na]
         if llist.size:
             h, b = llist[:, 0], llist[:, 1]
-            term = f32(0.5) * (B[h] * du[h] + D[h] * (f32(0.5) * (uh[b] - uh[l_node])))
-            np.add.at(acc, l_node, term)
-        dn = (acc * inv_m).astype(f32)
-        du[:na] = dn
-        y = (dn - uc[:na]).astype(f32)
-        tt = (uh[:na] + y).astype(f32)
-        uc[:na] = ((tt - uh[:na]).astype(f32) - y).astype(f32)
-        uh_new = uh.copy()
-        uh_new[:na] = tt
+            term = f32(0.5) * (E[h] * dh[h] + D[h] * (f32(0.5) * (uh[b] - uh[l_node]) + (dh[h] - dh[l_node])))
+            np.add.at(acc, l_node, term.astype(f32))
+        delta = (acc * inv_m).astype(f32)
+        # D+ = D + delta (Kahan, compensation rounded to `comp`)
+        y = (delta - dc[:na]).astype(f32)
+        tt = (dh[:na] + y).astype(f32)
+        dc[:na] = rnd(((tt - dh[:na]).astype(f32) - y).astype(f32))
+        dh[:na] = tt
+        # u+ = u + D+ (Kahan)
+        y = (tt - uc[:na]).astype(f32)
+        tu = (uh[:na] + y).astype(f32)
+        uc[:na] = rnd(((tu - uh[:na]).astype(f32) - y).astype(f32))
+        uh[:na] = tu
         if nh:
             a_, b_ = hang[:, 1], hang[:, 2]
-            uh_new[hang[:, 0]] = f32(0.5) * (uh_new[a_] + uh_new[b_])
-            uc[hang[:, 0]] = f32(0.5) * (uc[a_] + uc[b_])
-            du[hang[:, 0]] = f32(0.5) * (du[a_] + du[b_])
-        uh = uh_new
+            for arr in (uh, uc, dh, dc):
+                arr[hang[:, 0]] = f32(0.5) * (arr[a_] + arr[b_])
+            uc[hang[:, 0]] = rnd(uc[hang[:, 0]])
+            dc[hang[:, 0]] = rnd(dc[hang[:, 0]])
         if step % io == 0:
             sample(step // io)
     return {"seis": seis}

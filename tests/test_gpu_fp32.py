@@ -90,7 +90,8 @@ def test_fp32_vs_fp64_gpu_on_full_canyon():
 def test_diverging_run_is_reported():
     """dt five times over the stability limit: the watchdog turns the blow-up
     into EXFEM_E_NAN at sync instead of silent garbage."""
-    d = decks.homogeneous_rectangle(scale=0.125, steps=400).replace("CONTROL:\n10.0 2.0", "CONTROL:\n10.0 0.4")
+    d = decks.homogeneous_rectangle(scale=0.125, steps=400, save_every=10).replace("CONTROL:\n10.0 2.0",
+                                                                                    "CONTROL:\n10.0 0.4")
     m = Model(d)   # the deck's TIME now gives 80 steps of the larger dt
     with Solver(m, precision=EXFEM_FP32_KAHAN) as s:
         s.init_explicit()
