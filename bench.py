@@ -184,6 +184,36 @@ def cpu_baseline(m, target_s=12.0, rhs=0):
                       % (rhs, steps, m.problem.nsteps, m.nelems, nt)}
 
 
+def serving_leg(args, local):
+    """Bounded serving sample: Poisson arrivals of uneven canyon/valley
+    requests, FP32 with continuous batching, against the same requests run
+    serially in plain FP64 (one context at a time)."""
+    from exfem import decks
+    from exfem.gpu import Solver
+    from exfem.model import Model
+    from exfem.serve import run_stream
+    stream = decks.serving_stream(n=args.serve_requests, rate=20.0, seed=7, min_scale=0.2, max_scale=1.0,
+                                  max_angles=16, step_range=(500, 2000))
+    reqs = [(t, Model(d, nsteps=n, io_interval=4), n) for t, d, n in stream]
+    recs, summary, _ = run_stream(reqs, server_kw={"max_active": 16, "chunk_steps": 128, "device": local})
+    # plain FP64, serially, same requests
+    t0 = time.perf_counter()
+    work = 0
+    for _, m, n in reqs:
+        with Solver(m, device=local) as s:
+            s.init_explicit()
+            s.run(n)
+            s.seismograms()
+        work += m.nelems * m.problem.nrhs * n
+    t64 = time.perf_counter() - t0
+    sizes = [m.nelems for _, m, _ in reqs]
+    summary.update({"serial_fp64_throughput": work / t64, "serial_fp64_s": t64,
+                    "elements_min": min(sizes), "elements_max": max(sizes),
+                    "note": "latency = finish - arrival of a built model (host meshing excluded); "
+                            "%d requests, Poisson 20/s, 1-16 angles, 500-2000 steps" % len(reqs)})
+    return summary
+
+
 def run_reference(args, ws, rank, dist):
     if rank != 0:
         return
@@ -313,6 +343,8 @@ def run_ours(args, ws, rank, local, dist, torch):
                         "ratio_fp32_over_fp64": value / v64}
         del mf
 
+    serving = serving_leg(args, local) if args.serve_requests > 0 else None
+
     if rank != 0:
         return
     cpu = cpu_baseline(m) if ws == 1 else None
@@ -326,7 +358,7 @@ def run_ours(args, ws, rank, local, dist, torch):
                             % ((2 * m.nnodes * R * (8 if fp64 else 4) * (2 if fp64 else 4)) / 1e6),
                       "parallelism": "replicas" if ws > 1 else "single"},
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-           "tuned": tuned or None, "plain_fp64": fp64_ref}
+           "tuned": tuned or None, "plain_fp64": fp64_ref, "serving": serving}
     print(json.dumps(out))
 
 
@@ -343,6 +375,7 @@ def main():
                     help="timed loop only (no autotune, kernel profile, e2e, CPU or FP64 legs): for ncu captures")
     ap.add_argument("--block", type=int, default=0, help="force the step kernel's block size")
     ap.add_argument("--rpt", type=int, default=0, help="force right-hand sides per thread")
+    ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -502,6 +502,19 @@ int exfem_gpu_sync(exfem_ctx *ctx) {
     return EXFEM_OK;
 }
 
+int exfem_gpu_query(exfem_ctx *ctx) {
+    if (!ctx) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    CK(cudaSetDevice(c.device));
+    cudaError_t e = cudaStreamQuery(c.stream);
+    if (e == cudaErrorNotReady) return 1;
+    if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    int flag = 0;
+    CK(cudaMemcpy(&flag, c.dm.d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
+    return EXFEM_OK;
+}
+
 int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     if (!ctx || !u) return EXFEM_E_ARG;
     Ctx &c = *ctx;

@@ -57,7 +57,7 @@ def host_sources():
 def gpu_sources():
     srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
                   if f.endswith((".cu", ".cpp", ".cuh", ".h")))
-    return srcs + [os.path.join(INCLUDE, "exfem_gpu.h")]
+    return srcs + sorted(os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h"))
 
 
 def build_host(force=False):

@@ -81,6 +81,31 @@ class ModelInfo(C.Structure):
                 ("nlevels", C.c_int), ("min_h", C.c_double), ("max_h", C.c_double)]
 
 
+class SrvOpts(C.Structure):
+    _fields_ = [("hbm_budget", C.c_size_t), ("max_active", C.c_int), ("chunk_steps", C.c_int),
+                ("preparers", C.c_int), ("max_bypass", C.c_int), ("solver", Opts)]
+
+
+class SrvResult(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("status", C.c_int), ("nsteps", C.c_int), ("nelems", C.c_int),
+                ("nrhs", C.c_int), ("nrecv", C.c_int), ("nsave", C.c_int), ("device_bytes", C.c_size_t),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_ready", C.c_double),
+                ("t_done", C.c_double)]
+
+
+SRV_SYMBOLS = {
+    "exfem_srv_default_opts": (None, [C.POINTER(SrvOpts)]),
+    "exfem_srv_open": (C.c_int, [C.POINTER(SrvOpts), C.POINTER(C.c_void_p)]),
+    "exfem_srv_submit": (C.c_int, [C.c_void_p, C.POINTER(Mesh), C.POINTER(Problem), C.c_int,
+                                   C.POINTER(C.c_longlong)]),
+    "exfem_srv_poll": (C.c_int, [C.c_void_p, C.POINTER(SrvResult), C.c_int, C.c_int]),
+    "exfem_srv_fetch": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_double), C.c_size_t]),
+    "exfem_srv_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_longlong), C.POINTER(C.c_size_t), C.POINTER(C.c_int)]),
+    "exfem_srv_last_error": (C.c_char_p, [C.c_void_p]),
+    "exfem_srv_close": (None, [C.c_void_p]),
+}
+
 GPU_SYMBOLS = {
     "exfem_gpu_default_opts": (None, [C.POINTER(Opts)]),
     "exfem_gpu_create": (C.c_int, [C.POINTER(Mesh), C.POINTER(Problem), C.POINTER(Opts),
@@ -88,6 +113,7 @@ GPU_SYMBOLS = {
     "exfem_gpu_init_explicit": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "exfem_gpu_run": (C.c_int, [C.c_void_p, C.c_int]),
     "exfem_gpu_sync": (C.c_int, [C.c_void_p]),
+    "exfem_gpu_query": (C.c_int, [C.c_void_p]),
     "exfem_gpu_get_u": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t]),
     "exfem_gpu_get_seismograms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t,
                                             C.POINTER(C.c_int)]),

@@ -157,15 +157,19 @@ def valley_batched(scale=1.0, steps=20000, **kw):
 
 
 def serving_stream(n=512, rate=20.0, seed=7, min_scale=0.1, max_scale=1.0, max_angles=16,
-                   step_range=(1000, 20000)):
+                   step_range=(1000, 20000), canyon_nperlen=10.0, valley_chper=0.25):
     """Seeded request stream: (arrival_time, deck_text, nsteps) tuples.
 
-    Canyon radius 200-800 m or valley half-width 500-2500 m and depth
-    100-600 m, in a half-space; 1-16 incidence angles; Poisson arrivals."""
+    Each request is a canyon (radius 200-800 m) or a semi-elliptical valley
+    (half-width 500-2500 m, depth 100-600 m) in a half-space, with 1-16
+    incidence angles of one wave kind and Poisson arrivals at `rate` per second.
+    `scale` (uniform in [min_scale, max_scale]) sets the domain size; the
+    feature is clamped to fit its domain.  Mesh size grows with scale**2 and
+    with 1/chper**2 (valleys) or nperlen**2 (canyons)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
-    for i in range(n):
+    for _ in range(n):
         t += rng.exponential(1.0 / rate)
         s = float(rng.uniform(min_scale, max_scale))
         nang = int(rng.integers(1, max_angles + 1))
@@ -174,16 +178,14 @@ def serving_stream(n=512, rate=20.0, seed=7, min_scale=0.1, max_scale=1.0, max_a
         lim = 28.0 if kind == "WAVESV" else 70.0
         angles = sorted(float(a) for a in rng.uniform(0.0, lim, nang))
         if rng.random() < 0.5:
-            r = float(rng.uniform(200, 800))
-            waves = [(kind, a) for a in angles]
-            deck = canyon(scale=s, steps=steps, radius=r / max(s, 1e-9), waves=waves,
-                          refine_levels=1, nperlen=10.0)
+            r = min(float(rng.uniform(200, 800)), 0.3 * 3000.0 * s)
+            deck = canyon(scale=s, steps=steps, radius=r / s, waves=[(kind, a) for a in angles],
+                          refine_levels=1, nperlen=canyon_nperlen, save_every=4)
         else:
-            a = float(rng.uniform(500, 2500))
-            d = float(rng.uniform(100, 600))
+            a = min(float(rng.uniform(500, 2500)), 0.3 * 12000.0 * s)
+            d = min(float(rng.uniform(100, 600)), 0.2 * 4000.0 * s)
             rhs = [(kind, math.radians(x), 1.0, 5.0) for x in angles]
-            deck = valley(scale=s, steps=steps, chper=0.25, rhs=rhs, seed=int(rng.integers(1 << 30)),
-                          half_width=a / max(s, 1e-9) * min(1.0, 5000.0 / a),
-                          depth=d / max(s, 1e-9) * min(1.0, 1.0), sigma=0.1)
+            deck = valley(scale=s, steps=steps, chper=valley_chper, rhs=rhs, seed=int(rng.integers(1 << 30)),
+                          half_width=a / s, depth=d / s, sigma=0.1, save_every=4)
         out.append((t, deck, steps))
     return out

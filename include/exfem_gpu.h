@@ -141,6 +141,10 @@ int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out);
  * io_utils.f90:390).  Asynchronous: returns after queueing the work. */
 int exfem_gpu_run(exfem_ctx *ctx, int nsteps);
 
+/* Non-blocking: 0 when every queued step has finished, 1 while work is still
+ * running, or a negative code (EXFEM_E_NAN when the watchdog tripped). */
+int exfem_gpu_query(exfem_ctx *ctx);
+
 /* Wait for queued work; returns EXFEM_E_NAN if the watchdog tripped. */
 int exfem_gpu_sync(exfem_ctx *ctx);
 

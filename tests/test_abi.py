@@ -24,6 +24,14 @@ def test_gpu_library_exports_header_symbols():
         assert hasattr(lib, n), n
 
 
+def test_server_symbols_are_exported():
+    lib = C.CDLL(_native.GPU_LIB)
+    names = declared("exfem_srv.h")
+    assert len(names) >= 8
+    for n in names:
+        assert hasattr(lib, n), n
+
+
 def test_host_library_exports_header_symbols():
     lib = C.CDLL(_native.HOST_LIB)
     for n in declared("exfem_host.h"):

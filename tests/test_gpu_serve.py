@@ -1,0 +1,94 @@
+"""Serving (include/exfem_srv.h): continuous batching of uneven requests.
+
+Each request's seismograms must be the same in the mix as alone (FP32 form,
+1e-6: the contexts are independent, so in practice they are identical), and
+the FP32 results stay within 1e-4 of the FP64 oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from exfem import decks, workloads
+from exfem.abi import EXFEM_E_NOMEM, EXFEM_E_UNSUPPORTED, EXFEM_FP32_KAHAN
+from exfem.gpu import Solver, estimate_bytes
+from exfem.model import Model
+from exfem.serve import Server, run_stream
+from oracle import oracle
+from util import per_receiver_rel
+
+pytestmark = pytest.mark.gpu
+NT = os.cpu_count() or 8
+
+
+def mix():
+    out = []
+    for i, (arr, deck, steps) in enumerate(decks.serving_stream(n=6, seed=11, min_scale=0.08, max_scale=0.2,
+                                                                 max_angles=4, step_range=(200, 600))):
+        out.append((Model(deck, nsteps=steps, io_interval=4), steps))
+    return out
+
+
+def alone32(m, steps):
+    with Solver(m, precision=EXFEM_FP32_KAHAN) as s:
+        s.init_explicit()
+        s.run(steps)
+        s.sync()
+        return s.seismograms()[:, : steps // m.problem.io_interval + 1]
+
+
+def test_each_result_is_the_same_in_the_mix_as_alone():
+    reqs = mix()
+    with Server(max_active=4, chunk_steps=64) as srv:
+        ids = [srv.submit(m, n) for m, n in reqs]
+        res = srv.wait_all(len(ids))
+        assert len(res) == len(ids) and all(r["status"] == 0 for r in res)
+        got = {r["id"]: srv.fetch(r["id"]) for r in res}
+        assert srv.stats()["peak_active"] >= 2
+    for rid, (m, n) in zip(ids, reqs):
+        ref = alone32(m, n)
+        for r in range(m.problem.nrhs):
+            assert per_receiver_rel(got[rid][r], ref[r]).max() <= 1e-6
+    m, n = reqs[0]
+    o = oracle.run(m, rhs=0, nsteps=n, nthreads=NT)
+    assert per_receiver_rel(got[ids[0]][0], o["seis"]).max() <= 1e-4
+
+
+def test_admission_respects_the_hbm_budget():
+    reqs = mix()
+    est = [estimate_bytes(m, precision=EXFEM_FP32_KAHAN) for m, _ in reqs]
+    budget = int(sorted(est)[-1] + sorted(est)[-2] + 1)
+    with Server(hbm_budget=budget, max_active=8, chunk_steps=64) as srv:
+        ids = [srv.submit(m, n) for m, n in reqs]
+        res = srv.wait_all(len(ids))
+    assert all(r["status"] == 0 for r in res)
+    # at no time do the running requests' estimates exceed the budget
+    spans = [(r["t_admit"], r["t_done"], est[ids.index(r["id"])]) for r in res]
+    for t, _, _ in spans:
+        assert sum(b for a, d, b in spans if a <= t < d) <= budget
+
+
+def test_failures_stay_isolated():
+    good, n = mix()[0]
+    bad = Model(decks.homogeneous_rectangle(scale=0.125, steps=50, angle=0.6), nsteps=50)   # SV past critical
+    with Server(max_active=4) as srv:
+        a = srv.submit(good, n)
+        b = srv.submit(bad, 50)
+        res = {r["id"]: r for r in srv.wait_all(2)}
+    assert res[a]["status"] == 0 and res[b]["status"] == EXFEM_E_UNSUPPORTED
+
+
+def test_request_larger_than_the_budget_is_refused():
+    m, n = mix()[1]
+    with Server(hbm_budget=1 << 20, max_active=4) as srv:
+        rid = srv.submit(m, n)
+        res = srv.wait_all(1)
+    assert res[0]["id"] == rid and res[0]["status"] == EXFEM_E_NOMEM
+
+
+def test_timed_stream_reports_latency_and_throughput():
+    stream = decks.serving_stream(n=10, rate=40.0, seed=5, min_scale=0.06, max_scale=0.15, max_angles=3,
+                                  step_range=(100, 300))
+    reqs = [(t, Model(d, nsteps=s, io_interval=4), s) for t, d, s in stream]
+    recs, summary, _ = run_stream(reqs, server_kw={"max_active": 6, "chunk_steps": 64})
+    assert summary["ok"] == 10 and 0 < summary["p50_s"] <= summary["p99_s"]
+    assert summary["throughput"] > 0
