@@ -158,7 +158,7 @@ def ncu_traffic(kernel, workload):
     try:
         with open(os.path.join(HERE, "profiles", "ncu_traffic.json")) as f:
             d = json.load(f)
-        v = d.get(workload, {}).get(kernel)
+        v = d.get(workload, {}).get(kernel.split("<")[0])
         return v.get("bytes_per_launch") if isinstance(v, dict) else v
     except Exception:
         return None

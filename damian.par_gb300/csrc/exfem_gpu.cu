@@ -626,16 +626,29 @@ long long exfem_gpu_launch_count(const exfem_ctx *ctx) { return ctx ? ctx->launc
 size_t exfem_gpu_device_bytes(const exfem_ctx *ctx) { return ctx ? ctx->bytes : 0; }
 
 size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts) {
+    // An upper bound of what exfem_gpu_create and init_explicit allocate
+    // (the sum over the allocations of setup_device, alloc_fp64/f32_alloc).
     if (!mesh || !prob) return 0;
-    size_t nn = (size_t)std::max(mesh->nnodes, 0), ne = (size_t)std::max(mesh->nelems, 0);
-    size_t R = (size_t)std::max(prob->nrhs, 1);
-    size_t nsave = (size_t)(prob->io_interval > 0 ? prob->nsteps / prob->io_interval + 1 : 1);
-    bool f64 = !opts || opts->precision == EXFEM_FP64;
-    size_t b = ne * (16 + 32 + 16 + 8 + 4) + nn * (16 + 8 + 16 + 4 * 12) + (size_t)prob->nhanging * 12 * 8;
-    b += R * nsave * (size_t)prob->nrecv * 16 + (size_t)prob->nseismic * (8 * 8 * R + 8);
-    if (f64) b += R * (nn * 32 + ne * 64);
-    else b += R * nn * 24 + nn * 24;
-    return b + (1u << 20);
+    const size_t nn = (size_t)std::max(mesh->nnodes, 0), ne = (size_t)std::max(mesh->nelems, 0);
+    const size_t R = (size_t)std::max(prob->nrhs, 1), nh = (size_t)std::max(prob->nhanging, 0);
+    const size_t ns = (size_t)std::max(prob->nseismic, 0), nr = (size_t)std::max(prob->nrecv, 0);
+    const size_t nsave = prob->io_interval > 0 ? (size_t)(prob->nsteps / prob->io_interval + 1) : 1;
+    size_t nabs = 0;
+    if (prob->absorbing)
+        for (size_t i = 0; i < nn; ++i) nabs += prob->absorbing[i] != 0;
+    const bool f64 = !opts || opts->precision == EXFEM_FP64;
+    size_t b = 16 * nn;                                            // node coordinates
+    b += ne * (16 + 8 + 16 + 4 + 32 + 16);                         // conn, mass, (mu,l), damp slot, coef, own list
+    b += 64 * std::min(ne, 4 * nabs + 4);                          // dashpot values of boundary elements
+    b += 4 * (nn + 1) * 4 + 16 * nn + 16 * nh + 12 * nh;           // node lists, m_full, 1/m_full, links, hanging
+    b += 4 * (4 * ne + 4 * nh);                                    // gather lists (own + hanging halves)
+    b += ns * (16 + 8 + 32) + nr * (16 + 32 + 4 + 16) + R * 192;   // DRM lists, receivers, waves
+    b += 16 * std::max(ns, (size_t)1) * R * 8;                      // DRM forces
+    b += R * nsave * std::max(nr, (size_t)1) * 16 + 16;            // seismograms, counters
+    if (f64) b += R * (nn * 32 + ne * 64);                          // u ping-pong, element forces
+    else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 32 * std::max(ns, (size_t)1) * R +
+              R * nn * 2 * (4 + 4 + 2 + 4 + 2);                     // FP32 state
+    return b + 64 * 1024;
 }
 
 const char *exfem_gpu_last_error(const exfem_ctx *ctx) {

@@ -34,7 +34,7 @@ struct Req {
     std::vector<exfem_wave> waves;
     exfem_mesh mesh{};
     exfem_problem prob{};
-    size_t est = 0, held = 0;
+    size_t est = 0, held = 0, actual = 0;
     exfem_ctx *ctx = nullptr;
     int bypassed = 0;
     double t_submit = 0, t_admit = 0, t_ready = 0, t_done = 0;
@@ -145,9 +145,7 @@ struct exfem_srv {
                 finish(r, rc);
             } else {
                 r->ctx = ctx;
-                size_t actual = exfem_gpu_device_bytes(ctx);
-                held = held - std::min(held, r->held) + actual;   // replace the estimate
-                r->held = actual;
+                r->actual = exfem_gpu_device_bytes(ctx);   // the reservation stays at the estimate
                 r->t_ready = now();
                 r->state = ACTIVE;
                 active.push_back(r);
@@ -328,7 +326,8 @@ int exfem_srv_poll(exfem_srv *s, exfem_srv_result *out, int cap, int wait_ms) {
         o.nrhs = r->prob.nrhs;
         o.nrecv = r->prob.nrecv;
         o.nsave = r->prob.io_interval > 0 ? r->nsteps / r->prob.io_interval + 1 : 0;
-        o.device_bytes = r->est;
+        o.device_bytes = r->actual;
+        o.reserved_bytes = r->est;
         o.t_submit = r->t_submit;
         o.t_admit = r->t_admit;
         o.t_ready = r->t_ready;

@@ -89,6 +89,7 @@ class SrvOpts(C.Structure):
 class SrvResult(C.Structure):
     _fields_ = [("id", C.c_longlong), ("status", C.c_int), ("nsteps", C.c_int), ("nelems", C.c_int),
                 ("nrhs", C.c_int), ("nrecv", C.c_int), ("nsave", C.c_int), ("device_bytes", C.c_size_t),
+                ("reserved_bytes", C.c_size_t),
                 ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_ready", C.c_double),
                 ("t_done", C.c_double)]
 

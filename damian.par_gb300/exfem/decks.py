@@ -103,7 +103,8 @@ def canyon(scale=1.0, steps=8000, radius=500.0, nperlen=25.0, waves=None, refine
     pparams = [box_w, box_h, width / 2, 0.0, 1, rhs[0][4], rhs[0][1], 1.0, freq]
     ncol = 64
     dist = width / ncol
-    return _deck(width, height, steps * dt * 1.0000001, save_every * dt, 0.25, nperlen, 2,
+    # dt <= h/(vp*2) for any refinement: the save interval uses that bound
+    return _deck(width, height, steps * (h / 4000.0) * 1.0000001, save_every * (h / 4000.0), 0.25, nperlen, 2,
                  [ROCK_HALFSPACE], rhs[0][0], pparams, geom="CANYON",
                  gparams=(width / 2, 0.0, radius), receivers=(0.0, width - dist, dist), rhs=rhs,
                  refine=(refine_levels, refine_band * max(scale, 0.25)))
@@ -133,7 +134,7 @@ def valley(scale=1.0, steps=20000, chper=0.056, rhs=None, seed=2024, sigma=0.1, 
     pparams = [box_w, box_h, width / 2, 0.0, 1, rhs[0][4], rhs[0][1], 1.0, rhs[0][3]]
     ncol = 64
     dist = width / ncol
-    return _deck(width, height, steps * dt_up, save_every * dt_up / 64.0, chper, 10, 2, VALLEY_MATERIALS,
+    return _deck(width, height, steps * dt_up, save_every * dt_up, chper, 10, 2, VALLEY_MATERIALS,
                  rhs[0][0], pparams, geom="EVALLY", gparams=(width / 2, 0.0, a, b),
                  receivers=(0.0, width - dist, dist), rhs=rhs,
                  heterogeneity=(sigma, seed) if sigma > 0 else None)

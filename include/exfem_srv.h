@@ -41,7 +41,8 @@ typedef struct exfem_srv_result {
     long long id;
     int       status;      /* EXFEM_OK or the request's EXFEM_E_* code             */
     int       nsteps, nelems, nrhs, nrecv, nsave;
-    size_t    device_bytes;
+    size_t    device_bytes;    /* bytes its context held                        */
+    size_t    reserved_bytes;  /* footprint reserved at admission (upper bound)  */
     double    t_submit, t_admit, t_ready, t_done;
 } exfem_srv_result;
 

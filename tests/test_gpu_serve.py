@@ -61,8 +61,10 @@ def test_admission_respects_the_hbm_budget():
         ids = [srv.submit(m, n) for m, n in reqs]
         res = srv.wait_all(len(ids))
     assert all(r["status"] == 0 for r in res)
-    # at no time do the running requests' estimates exceed the budget
-    spans = [(r["t_admit"], r["t_done"], est[ids.index(r["id"])]) for r in res]
+    for r in res:   # the reservation bounds what the context really held
+        assert r["reserved_bytes"] == est[ids.index(r["id"])] >= r["device_bytes"] > 0
+    # at no time do the reservations of running requests exceed the budget
+    spans = [(r["t_admit"], r["t_done"], r["reserved_bytes"]) for r in res]
     for t, _, _ in spans:
         assert sum(b for a, d, b in spans if a <= t < d) <= budget
 
