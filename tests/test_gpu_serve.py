@@ -81,7 +81,7 @@ def test_failures_stay_isolated():
 
 def test_request_larger_than_the_budget_is_refused():
     m, n = mix()[1]
-    with Server(hbm_budget=1 << 20, max_active=4) as srv:
+    with Server(hbm_budget=4096, max_active=4) as srv:
         rid = srv.submit(m, n)
         res = srv.wait_all(1)
     assert res[0]["id"] == rid and res[0]["status"] == EXFEM_E_NOMEM
