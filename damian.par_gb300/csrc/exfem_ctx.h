@@ -20,6 +20,7 @@ struct DevWave {
     double amp0, wa1, wb1;
     double wui[6];
     double t0;
+    double inv_alpha, inv_beta;   // 1/vp, 1/vs (FP32 free field only)
 };
 
 // Device arrays common to both arithmetic forms.

@@ -53,9 +53,10 @@ __host__ __device__ __forceinline__ void q4_ku_corner(T A, T B, T C, T D, const 
 
 // Consistent mass (calcsqm/9, formulation.f90:256-268) times v for one
 // component: weights 4 (self), 2 (edge neighbours), 1 (opposite corner).
-__host__ __device__ __forceinline__ void q4_msq(const double v[4], double out[4]) {
+template <typename T>
+__host__ __device__ __forceinline__ void q4_msq(const T v[4], T out[4]) {
     for (int k = 0; k < 4; ++k)
-        out[k] = (4.0 * v[k] + 2.0 * v[(k + 1) & 3] + v[(k + 2) & 3] + 2.0 * v[(k + 3) & 3]) / 9.0;
+        out[k] = (T(4) * v[k] + T(2) * v[(k + 1) & 3] + v[(k + 2) & 3] + T(2) * v[(k + 3) & 3]) / T(9);
 }
 
 // One Ricker term with its first two time derivatives (pwaves.f90:157-169).
@@ -69,7 +70,6 @@ __host__ __device__ __forceinline__ void ricker3(double fp, double d, double out
 }
 
 // planewave (pwaves.f90:100-217): u[comp][col], comp x/z, col u/du/ddu.
-// `ncol` limits the work to the first columns needed (1: displacement only).
 __host__ __device__ __forceinline__ void planewave(const DevWave &w, double t, double x1, double x3, double ux[3],
                                           double uz[3]) {
     double v0;
@@ -122,34 +122,64 @@ __host__ __device__ __forceinline__ unsigned drm_mask(int kind) {
 // model.f90:745-800, with multdrm formulation.f90:378-393 for K and for the
 // consistent mass): p = -K_be u0_e on boundary dofs, +K_eb u0_b on exterior
 // dofs, plus the same with M_cons*mass on the free-field acceleration.
-__host__ __device__ __forceinline__ void drm_forces(const double k[4], double mass, unsigned e, const double u0[8],
-                                           const double a0[8], double p[8]) {
-    double uex[4], uey[4], ubx[4], uby[4];
+template <typename T>
+__host__ __device__ __forceinline__ void drm_forces(const T k[4], T mass, unsigned e, const T u0[8], const T a0[8],
+                                                    T p[8]) {
+    T uex[4], uey[4], ubx[4], uby[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         bool ex = (e >> (2 * c)) & 1u, ey = (e >> (2 * c + 1)) & 1u;
-        uex[c] = ex ? u0[2 * c] : 0.0;       ubx[c] = ex ? 0.0 : u0[2 * c];
-        uey[c] = ey ? u0[2 * c + 1] : 0.0;   uby[c] = ey ? 0.0 : u0[2 * c + 1];
+        uex[c] = ex ? u0[2 * c] : T(0);       ubx[c] = ex ? T(0) : u0[2 * c];
+        uey[c] = ey ? u0[2 * c + 1] : T(0);   uby[c] = ey ? T(0) : u0[2 * c + 1];
     }
-    double kex[4], key[4], kbx[4], kby[4];
-    q4_ku<double>(k[0], k[1], k[2], k[3], uex, uey, kex, key);
-    q4_ku<double>(k[0], k[1], k[2], k[3], ubx, uby, kbx, kby);
-    double aex[4], aey[4], abx[4], aby[4];
+    T kex[4], key[4], kbx[4], kby[4];
+    q4_ku<T>(k[0], k[1], k[2], k[3], uex, uey, kex, key);
+    q4_ku<T>(k[0], k[1], k[2], k[3], ubx, uby, kbx, kby);
+    T aex[4], aey[4], abx[4], aby[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         bool ex = (e >> (2 * c)) & 1u, ey = (e >> (2 * c + 1)) & 1u;
-        aex[c] = ex ? a0[2 * c] : 0.0;       abx[c] = ex ? 0.0 : a0[2 * c];
-        aey[c] = ey ? a0[2 * c + 1] : 0.0;   aby[c] = ey ? 0.0 : a0[2 * c + 1];
+        aex[c] = ex ? a0[2 * c] : T(0);       abx[c] = ex ? T(0) : a0[2 * c];
+        aey[c] = ey ? a0[2 * c + 1] : T(0);   aby[c] = ey ? T(0) : a0[2 * c + 1];
     }
-    double mex[4], mey[4], mbx[4], mby[4];
-    q4_msq(aex, mex); q4_msq(aey, mey); q4_msq(abx, mbx); q4_msq(aby, mby);
+    T mex[4], mey[4], mbx[4], mby[4];
+    q4_msq<T>(aex, mex); q4_msq<T>(aey, mey); q4_msq<T>(abx, mbx); q4_msq<T>(aby, mby);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         bool ex = (e >> (2 * c)) & 1u, ey = (e >> (2 * c + 1)) & 1u;
-        double pkx = ex ? kbx[c] : -kex[c], pky = ey ? kby[c] : -key[c];
-        double pmx = ex ? mbx[c] : -mex[c], pmy = ey ? mby[c] : -mey[c];
+        T pkx = ex ? kbx[c] : -kex[c], pky = ey ? kby[c] : -key[c];
+        T pmx = ex ? mbx[c] : -mex[c], pmy = ey ? mby[c] : -mey[c];
         p[2 * c] = pkx + pmx * mass;
         p[2 * c + 1] = pky + pmy * mass;
+    }
+}
+
+// Free-field displacement and acceleration for the FP32 form: the travel
+// time t - (x sin + z cos)/v is formed in FP64 (the subtraction cancels), the
+// Ricker terms in FP32.  Relative error ~1e-7, the size of storing the forces
+// in FP32.
+__host__ __device__ __forceinline__ void planewave32(const DevWave &w, double t, double x1, double x3, float u[2],
+                                                     float a[2]) {
+    double v[3];
+    if (w.kind == EXFEM_WAVE_P) v[0] = (x1 * w.sine - x3 * w.cose) * w.inv_alpha;
+    else v[0] = (x1 * w.sinf - x3 * w.cosf) * w.inv_beta;
+    v[1] = (x1 * w.sine + x3 * w.cose) * w.inv_alpha;
+    v[2] = (x1 * w.sinf + x3 * w.cosf) * w.inv_beta;
+    const float fp2 = (float)(w.fp * w.fp);
+    const float amp[3] = {(float)w.amp0, (float)w.wa1, (float)w.wb1};
+    u[0] = u[1] = a[0] = a[1] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float q = (float)(w.fp * (t - v[k]));
+        float s2 = q * q;
+        float e = expf(-s2);
+        float r0 = (1.f - 2.f * s2) * e;
+        float r2 = -2.f * ((4.f * s2 - 12.f) * s2 + 3.f) * fp2 * e;
+        float ax = (float)w.wui[2 * k] * amp[k], az = (float)w.wui[2 * k + 1] * amp[k];
+        u[0] += r0 * ax;
+        u[1] += r0 * az;
+        a[0] += r2 * ax;
+        a[1] += r2 * az;
     }
 }
 

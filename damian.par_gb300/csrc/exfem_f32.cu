@@ -134,29 +134,28 @@ __device__ __forceinline__ unsigned short f2bf(float f) { return __bfloat16_as_u
 
 __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
 
-// DRM forces (model.f90:745-800) in FP64, stored FP32.
+// DRM forces (model.f90:745-800) for the FP32 form: travel times in FP64,
+// the Ricker terms and the boundary/exterior split in FP32.
 __global__ void k_drm32(DevModel m) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m.ns * m.R) return;
     int s = (int)(t / m.R), r = (int)(t % m.R);
     int step = read_step(m) + 1;
-    const DevWave w = m.waves[r];
+    const DevWave &w = m.waves[r];
     double outt = (double)step * m.dt - w.t0;
     int ie = m.s_elem[s];
-    double u0[8], a0[8];
+    float u0[8], a0[8];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int x = m.econn[4 * ie + k];
-        double ux[3], uz[3];
-        planewave(w, outt, m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, ux, uz);
-        u0[2 * k] = ux[0]; u0[2 * k + 1] = uz[0];
-        a0[2 * k] = ux[2]; a0[2 * k + 1] = uz[2];
+        planewave32(w, outt, m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, &u0[2 * k], &a0[2 * k]);
     }
-    double kc[4] = {m.ecoef[4 * ie], m.ecoef[4 * ie + 1], m.ecoef[4 * ie + 2], m.ecoef[4 * ie + 3]};
-    double p[8];
-    drm_forces(kc, m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
+    const float4 k4 = reinterpret_cast<const float4 *>(m.ecoef32)[ie];
+    float kc[4] = {k4.x, k4.y, k4.z, k4.w};
+    float p[8];
+    drm_forces<float>(kc, (float)m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) m.fdrm32[((size_t)s * 8 + k) * m.R + r] = (float)p[k];
+    for (int k = 0; k < 8; ++k) m.fdrm32[((size_t)s * 8 + k) * m.R + r] = p[k];
 }
 
 // The fused step for one non-hanging node and RPT right-hand sides.

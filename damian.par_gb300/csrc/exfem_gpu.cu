@@ -68,7 +68,7 @@ __global__ void k_drm(DevModel m) {
     }
     double kc[4] = {m.ecoef[4 * ie], m.ecoef[4 * ie + 1], m.ecoef[4 * ie + 2], m.ecoef[4 * ie + 3]};
     double p[8];
-    drm_forces(kc, m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
+    drm_forces<double>(kc, m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
 #pragma unroll
     for (int k = 0; k < 8; ++k) m.fdrm[((size_t)s * 16 + k) * m.R + r] = p[k];
 }
@@ -268,6 +268,8 @@ int setup_device(Ctx &c) {
         d.amp0 = w.amp0; d.wa1 = w.wa1; d.wb1 = w.wb1;
         for (int k = 0; k < 6; ++k) d.wui[k] = w.wui[k];
         d.t0 = w.t0;
+        d.inv_alpha = 1.0 / w.alpha;
+        d.inv_beta = 1.0 / w.beta;
     }
     TRY(upload(c, dw, &m.waves));
     TRY(dalloc(c, (size_t)std::max(m.ns, 1) * 16 * P.R, &m.fdrm));

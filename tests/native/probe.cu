@@ -19,6 +19,8 @@ DevWave to_dev(const WaveConst &w) {
     d.amp0 = w.amp0; d.wa1 = w.wa1; d.wb1 = w.wb1;
     for (int k = 0; k < 6; ++k) d.wui[k] = w.wui[k];
     d.t0 = w.t0;
+    d.inv_alpha = 1.0 / w.alpha;
+    d.inv_beta = 1.0 / w.beta;
     return d;
 }
 }  // namespace
@@ -41,7 +43,7 @@ void probe_q4_ku_f32(float A, float B, float C, float D, const float *ux, const 
 }
 
 void probe_drm_forces(const double *k4, double mass, int kind, const double *u0, const double *a0, double *p) {
-    drm_forces(k4, mass, drm_mask(kind), u0, a0, p);
+    drm_forces<double>(k4, mass, drm_mask(kind), u0, a0, p);
 }
 
 int probe_planewave(int kind, double amp, double alpha, double beta, double angle, double freq, double t, double x1,
@@ -54,6 +56,18 @@ int probe_planewave(int kind, double amp, double alpha, double beta, double angl
     double ux[3], uz[3];
     planewave(d, t, x1, x3, ux, uz);
     for (int c = 0; c < 3; ++c) { u6[2 * c] = ux[c]; u6[2 * c + 1] = uz[c]; }
+    return 0;
+}
+
+// The FP32 free field of the FP32 form: u2 = (ux, uz), a2 = (ax, az).
+int probe_planewave32(int kind, double amp, double alpha, double beta, double angle, double freq, double t, double x1,
+                      double x3, float *u2, float *a2) {
+    exfem_wave w{kind, amp, angle, freq, 0.0};
+    WaveConst wc;
+    int rc = init_wave_const(w, alpha, beta, wc, g_err);
+    if (rc) return rc;
+    DevWave d = to_dev(wc);
+    planewave32(d, t, x1, x3, u2, a2);
     return 0;
 }
 

@@ -45,6 +45,8 @@ def lib():
     L.probe_drm_forces.argtypes = [d, C.c_double, C.c_int, d, d, d]
     L.probe_planewave.restype = C.c_int
     L.probe_planewave.argtypes = [C.c_int] + [C.c_double] * 8 + [d]
+    L.probe_planewave32.restype = C.c_int
+    L.probe_planewave32.argtypes = [C.c_int] + [C.c_double] * 8 + [f, f]
     L.probe_planewave_u.restype = C.c_int
     L.probe_planewave_u.argtypes = [C.c_int] + [C.c_double] * 8 + [d]
     L.probe_plan.restype = C.c_void_p

@@ -1,5 +1,6 @@
 """The library's __host__ __device__ arithmetic and plan builder, compiled
 for the host (tests/native/probe.cu), against the oracle."""
+import ctypes as C
 import math
 
 import numpy as np
@@ -67,6 +68,20 @@ def test_device_planewave_matches_oracle(kind, deg):
             d = np.zeros(2)
             L.probe_planewave_u(kind, 1.3, 2000.0, 1000.0, math.radians(deg), 3.0, t, x1, x3, npb.dp(d))
             assert np.allclose(d, want[:, 0], rtol=1e-14, atol=1e-15)
+
+
+@pytest.mark.parametrize("kind,deg", [(EXFEM_WAVE_P, 40), (EXFEM_WAVE_SV, 20)])
+def test_fp32_free_field_matches_fp64(kind, deg):
+    L = npb.lib()
+    for t in (-0.3, 0.0, 0.21, 1.7):
+        for x1, x3 in ((0.0, 0.0), (-1900.0, 700.0), (2500.0, 1800.0)):
+            want = oracle.planewave(kind, 1.0, 3000.0, 1500.0, math.radians(deg), 5.0, t, x1, x3)
+            u, a = np.zeros(2, np.float32), np.zeros(2, np.float32)
+            fp = C.POINTER(C.c_float)
+            assert L.probe_planewave32(kind, 1.0, 3000.0, 1500.0, math.radians(deg), 5.0, t, x1, x3,
+                                       u.ctypes.data_as(fp), a.ctypes.data_as(fp)) == 0
+            assert np.allclose(u, want[:, 0], rtol=0, atol=2e-6 * max(1.0, np.abs(want[:, 0]).max()))
+            assert np.allclose(a, want[:, 2], rtol=0, atol=2e-6 * np.abs(want[:, 2]).max() + 1e-3)
 
 
 def test_device_wave_setup_rejects_unsupported_angles():
