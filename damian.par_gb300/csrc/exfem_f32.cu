@@ -169,6 +169,21 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     const int n = (int)(t / G);
     const int r0 = (int)(t % G) * RPT;
     const size_t R = m.R;
+    const size_t bn = ((size_t)n * 2) * R + r0;
+    // Ask L2 for this node's own streaming state (read only after the
+    // gather) so its DRAM latency overlaps the gather instead of following
+    // it.  Measured on the 64-RHS valley: 8% faster at 4 and 1 right-hand
+    // sides per thread, slower at 2, where it is left out.
+    if (RPT != 2) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dh + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dh + bn + R));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dc + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dc + bn + R));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(uc + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(uc + bn + R));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(uh + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(uh + bn + R));
+    }
     float ax[RPT], ay[RPT];
 #pragma unroll
     for (int j = 0; j < RPT; ++j) { ax[j] = 0.f; ay[j] = 0.f; }
@@ -214,7 +229,6 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     }
     // dashpot term -2 a2 C D (zero away from the absorbing boundary)
     const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
-    const size_t bn = ((size_t)n * 2) * R + r0;
     float dx[RPT], dy[RPT];
     Vec<RPT>::load_cg(dh + bn, dx);
     Vec<RPT>::load_cg(dh + bn + R, dy);
