@@ -254,13 +254,16 @@ def run_ours(args, ws, rank, local, dist, torch):
     m = workloads.build(args.workload, scale=args.scale, steps=max(total, 8))
     R = m.problem.nrhs
     tuned = {}
-    if args.block or args.rpt:
+    if args.block or args.rpt or args.variant >= 0:
         tuned = {k: v for k, v in (("block_threads", args.block), ("rhs_per_thread", args.rpt)) if v}
+        if args.variant >= 0:
+            tuned["variant"] = args.variant
     elif not fp64 and not args.no_extras:
         from exfem import autotune
         mt = workloads.build(args.workload, scale=args.scale, steps=24)
         choice = autotune.tune(mt, steps=10, warmup=3, device=local)
-        tuned = {"block_threads": choice["block_threads"], "rhs_per_thread": choice["rhs_per_thread"]}
+        tuned = {"variant": choice["variant"], "block_threads": choice["block_threads"],
+                 "rhs_per_thread": choice["rhs_per_thread"]}
         del mt
     s = Solver(m, precision=form, device=local, **tuned)
     s.init_explicit()
@@ -375,6 +378,7 @@ def main():
                     help="timed loop only (no autotune, kernel profile, e2e, CPU or FP64 legs): for ncu captures")
     ap.add_argument("--block", type=int, default=0, help="force the step kernel's block size")
     ap.add_argument("--rpt", type=int, default=0, help="force right-hand sides per thread")
+    ap.add_argument("--variant", type=int, default=-1, help="force the kernel variant (FP32: 0 tiled, 1 direct)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     args = ap.parse_args()

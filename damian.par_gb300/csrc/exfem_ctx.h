@@ -80,6 +80,12 @@ struct Ctx {
     unsigned short *ucomp = nullptr;
     float *udel[2] = {nullptr, nullptr};
     unsigned short *dcomp = nullptr;
+    // shared-memory tiles of the FP32 step (see build_tiles)
+    bool use_tiles = false;
+    int tile_tn = 0, tile_n = 0, tile_hmax = 0, tile_rc = 0;
+    size_t tile_smem = 0;
+    const int *t_hptr = nullptr, *t_hlist = nullptr, *t_nslot = nullptr, *t_lslot = nullptr;
+    const unsigned short *t_tslot = nullptr;
     int parity = 0;          // index of the current u buffer
     int steps_done = 0;
     bool inited = false;

@@ -86,6 +86,28 @@ struct Vec<4> {
     }
 };
 
+// RPT floats from shared memory.
+template <int N>
+struct VecS;
+template <>
+struct VecS<1> {
+    __device__ static void load(const float *p, float *v) { v[0] = *p; }
+};
+template <>
+struct VecS<2> {
+    __device__ static void load(const float *p, float *v) {
+        float2 a = *reinterpret_cast<const float2 *>(p);
+        v[0] = a.x; v[1] = a.y;
+    }
+};
+template <>
+struct VecS<4> {
+    __device__ static void load(const float *p, float *v) {
+        float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+};
+
 // RPT bf16 values (raw 16-bit words) <-> float.
 template <int N>
 struct Half;
@@ -290,6 +312,156 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     Vec<RPT>::store(uhn + bn + R, oy);
 }
 
+// Tiled variant of k_step32: a block owns `tn` consecutive active nodes (a
+// compact Morton patch) and a chunk of `rc` right-hand sides.  It first copies
+// the u_hi rows of the patch's halo (every node its terms read) into shared
+// memory with coalesced vector loads, then each thread gathers its element
+// terms from shared memory through the host-computed halo slots.  The update
+// itself is the one of k_step32.
+struct TileArgs {
+    const int *hptr, *hlist, *nslot, *lslot;
+    const unsigned short *tslot;
+    int tn, rc;
+};
+
+template <int RPT>
+__global__ void __launch_bounds__(512) k_tile32(DevModel m, TileArgs ta, const float *__restrict__ uh,
+                                                float *__restrict__ uhn, unsigned short *__restrict__ uc,
+                                                float *__restrict__ dh, unsigned short *__restrict__ dc) {
+    extern __shared__ float sm[];
+    const int RC = ta.rc, G = RC / RPT, row = 2 * RC;
+    const int tile = blockIdx.x, rbase = blockIdx.y * RC;
+    const int h0 = ta.hptr[tile], nhalo = ta.hptr[tile + 1] - h0;
+    const size_t R = m.R;
+    const int ln = threadIdx.x / G, g = threadIdx.x - (threadIdx.x / G) * G;
+    const int n = tile * ta.tn + ln;
+    const bool valid = (ln < ta.tn) && (n < m.n_active);
+    const int rl = g * RPT, r0 = rbase + rl;
+    const size_t bn = ((size_t)n * 2) * R + r0;
+    if (valid && RPT != 2) {   // the node's own streaming state, as in k_step32
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dh + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dh + bn + R));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dc + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(dc + bn + R));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(uc + bn));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(uc + bn + R));
+    }
+    // halo rows -> shared memory
+    if ((RC & 3) == 0) {
+        const int per = row >> 2;
+        for (int i = threadIdx.x; i < nhalo * per; i += blockDim.x) {
+            int h = i / per, k = (i - h * per) << 2;
+            int d = k >= RC ? 1 : 0, rr = k - d * RC;
+            float4 v = __ldg(reinterpret_cast<const float4 *>(uh + ((size_t)__ldg(ta.hlist + h0 + h) * 2 + d) * R + rbase + rr));
+            *reinterpret_cast<float4 *>(sm + h * row + k) = v;
+        }
+    } else {
+        for (int i = threadIdx.x; i < nhalo * row; i += blockDim.x) {
+            int h = i / row, k = i - h * row;
+            int d = k >= RC ? 1 : 0, rr = k - d * RC;
+            sm[h * row + k] = __ldg(uh + ((size_t)__ldg(ta.hlist + h0 + h) * 2 + d) * R + rbase + rr);
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+    float ax[RPT], ay[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) { ax[j] = 0.f; ay[j] = 0.f; }
+    for (int q = m.dptr[n]; q < m.dptr[n + 1]; ++q) {
+        int ent = __ldg(m.dlist + q);
+        float w = (ent & 1) ? 0.5f : 1.0f;
+        int sc = ent >> 1;
+        size_t b = ((size_t)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
+        float fx[RPT], fy[RPT];
+        Vec<RPT>::load_cg(m.fdrm32 + b, fx);
+        Vec<RPT>::load_cg(m.fdrm32 + b + R, fy);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
+    }
+    const float4 *coef4 = reinterpret_cast<const float4 *>(m.ecoef32);
+    const ushort4 *slots = reinterpret_cast<const ushort4 *>(ta.tslot);
+    for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
+        int ent = __ldg(m.tlist + q);
+        float w = (ent & 1) ? 0.5f : 1.0f;
+        int ec = ent >> 1;
+        int e = ec >> 2, c = ec & 3;
+        float4 k = __ldg(coef4 + e);
+        ushort4 sl = __ldg(slots + q);
+        const int ss[4] = {sl.x, sl.y, sl.z, sl.w};
+        float ux[4][RPT], uy[4][RPT];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            VecS<RPT>::load(sm + ss[v] * row + rl, ux[v]);
+            VecS<RPT>::load(sm + ss[v] * row + RC + rl, uy[v]);
+        }
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
+            float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
+            float fx, fy;
+            q4_ku_corner<float>(k.x, k.y, k.z, k.w, vx, vy, c, fx, fy);
+            ax[j] -= w * fx;
+            ay[j] -= w * fy;
+        }
+    }
+    const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
+    float dx[RPT], dy[RPT];
+    Vec<RPT>::load_cg(dh + bn, dx);
+    Vec<RPT>::load_cg(dh + bn + R, dy);
+    if (nc.z != 0.f || nc.w != 0.f) {
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
+    }
+    const int ns_ = __ldg(ta.nslot + n);
+    float unx[RPT], uny[RPT];
+    VecS<RPT>::load(sm + ns_ * row + rl, unx);
+    VecS<RPT>::load(sm + ns_ * row + RC + rl, uny);
+    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
+        int h = __ldg(m.llist + 2 * q);
+        int sb = __ldg(ta.lslot + q);
+        float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
+        size_t bh = ((size_t)h * 2) * R + r0;
+        float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
+        Vec<RPT>::load_cg(dh + bh, hx);
+        Vec<RPT>::load_cg(dh + bh + R, hy);
+        VecS<RPT>::load(sm + sb * row + rl, ubx);
+        VecS<RPT>::load(sm + sb * row + RC + rl, uby);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j]) + (hx[j] - dx[j])));
+            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j]) + (hy[j] - dy[j])));
+        }
+    }
+    float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
+    Half<RPT>::load(dc + bn, dcx);
+    Half<RPT>::load(dc + bn + R, dcy);
+    Half<RPT>::load(uc + bn, ucx);
+    Half<RPT>::load(uc + bn + R, ucy);
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        float yx = ax[j] * nc.x - dcx[j], yy = ay[j] * nc.y - dcy[j];
+        float tx = dx[j] + yx, ty = dy[j] + yy;
+        dcx[j] = (tx - dx[j]) - yx;
+        dcy[j] = (ty - dy[j]) - yy;
+        dx[j] = tx;
+        dy[j] = ty;
+        float vx = tx - ucx[j], vy = ty - ucy[j];
+        float sx = unx[j] + vx, sy = uny[j] + vy;
+        ucx[j] = (sx - unx[j]) - vx;
+        ucy[j] = (sy - uny[j]) - vy;
+        ox[j] = sx;
+        oy[j] = sy;
+    }
+    Vec<RPT>::store(dh + bn, dx);
+    Vec<RPT>::store(dh + bn + R, dy);
+    Half<RPT>::store(dc + bn, dcx);
+    Half<RPT>::store(dc + bn + R, dcy);
+    Half<RPT>::store(uc + bn, ucx);
+    Half<RPT>::store(uc + bn + R, ucy);
+    Vec<RPT>::store(uhn + bn, ox);
+    Vec<RPT>::store(uhn + bn + R, oy);
+}
+
 // u of one node in FP64 (u_hi - comp); hanging corners read as anchor averages.
 __device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, const unsigned short *uc, int node,
                                          int r, double &vx, double &vy) {
@@ -441,6 +613,40 @@ int f32_alloc(Ctx &c) {
     if ((rc = alloc32(c, nst, &c.dcomp))) return rc;
     c.rhs_per_thread = pick_rpt(c);
     if (c.opts.block_threads <= 0) c.block_threads = 256;
+    // shared-memory tiles (variant 1; variant 0, the default, is the direct gather)
+    c.use_tiles = false;
+    if (c.opts.variant == 1) {
+        const int R = P.R, rpt = c.rhs_per_thread;
+        const int chunk = R <= 64 ? R : ((R % 64 == 0) ? 64 : 0);
+        if (chunk > 0 && chunk % rpt == 0) {
+            int G = chunk / rpt;
+            int tn = std::max(1, c.block_threads / G);
+            Tiles T;
+            std::string terr;
+            if (build_tiles(P, tn, T, terr) == EXFEM_OK) {
+                size_t smem = (size_t)T.hmax * 2 * chunk * sizeof(float);
+                int dev_smem = 0;
+                cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
+                if (smem <= (size_t)dev_smem && tn * G <= 512) {
+                    if ((rc = upload32(c, T.hptr, &c.t_hptr)) ||
+                        (rc = upload32(c, T.hlist, &c.t_hlist)) ||
+                        (rc = upload32(c, T.tslot, &c.t_tslot)) ||
+                        (rc = upload32(c, T.nslot, &c.t_nslot)))
+                        return rc;
+                    if (!T.lslot.empty() && (rc = upload32(c, T.lslot, &c.t_lslot))) return rc;
+                    c.tile_tn = tn;
+                    c.tile_n = T.ntiles;
+                    c.tile_hmax = T.hmax;
+                    c.tile_rc = chunk;
+                    c.tile_smem = smem;
+                    c.use_tiles = true;
+                    CK(cudaFuncSetAttribute(k_tile32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                    CK(cudaFuncSetAttribute(k_tile32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                    CK(cudaFuncSetAttribute(k_tile32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                }
+            }
+        }
+    }
     return EXFEM_OK;
 }
 
@@ -465,6 +671,18 @@ int f32_launch_step(Ctx &c, int par) {
     const int T = c.block_threads;
     const int rpt = c.rhs_per_thread;
     long long work = (long long)m.n_active * (m.R / rpt);
+    if (c.use_tiles) {
+        TileArgs ta{c.t_hptr, c.t_hlist, c.t_nslot, c.t_lslot, c.t_tslot, c.tile_tn, c.tile_rc};
+        dim3 grid(c.tile_n, m.R / c.tile_rc);
+        int threads = c.tile_tn * (c.tile_rc / rpt);
+        switch (rpt) {
+            case 4: k_tile32<4><<<grid, threads, c.tile_smem, c.stream>>>(m, ta, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            case 2: k_tile32<2><<<grid, threads, c.tile_smem, c.stream>>>(m, ta, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            default: k_tile32<1><<<grid, threads, c.tile_smem, c.stream>>>(m, ta, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        }
+        c.launches++;
+        mark(c, "k_tile32");
+    } else {
     switch (rpt) {
         case 4: k_step32<4><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
         case 2: k_step32<2><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
@@ -472,6 +690,7 @@ int f32_launch_step(Ctx &c, int par) {
     }
     c.launches++;
     mark(c, "k_step32");
+    }
     const int TH = 256;
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + TH - 1) / TH);
     int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);

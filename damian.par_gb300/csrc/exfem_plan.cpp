@@ -436,4 +436,45 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     return EXFEM_OK;
 }
 
+int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
+    if (tn < 1) { err = "tile size must be positive"; return EXFEM_E_ARG; }
+    T = Tiles();
+    T.tn = tn;
+    T.ntiles = (P.n_active + tn - 1) / tn;
+    T.hptr.assign(T.ntiles + 1, 0);
+    T.tslot.assign(4 * P.tlist.size(), 0);
+    T.nslot.assign(P.n_active, 0);
+    T.lslot.assign(P.llist.size() / 2, 0);
+    std::vector<int> slot(P.nn, -1), nodes;
+    for (int t = 0; t < T.ntiles; ++t) {
+        int n0 = t * tn, n1 = std::min(P.n_active, n0 + tn);
+        nodes.clear();
+        for (int n = n0; n < n1; ++n) {
+            nodes.push_back(n);
+            for (int q = P.tptr[n]; q < P.tptr[n + 1]; ++q) {
+                int e = (P.tlist[q] >> 1) >> 2;
+                for (int v = 0; v < 4; ++v) nodes.push_back(P.econn[(size_t)e * 4 + v]);
+            }
+            for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) nodes.push_back(P.llist[2 * (size_t)q + 1]);
+        }
+        std::sort(nodes.begin(), nodes.end());
+        nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
+        if (nodes.size() > 65535) { err = "tile halo too large"; return EXFEM_E_ARG; }
+        for (size_t i = 0; i < nodes.size(); ++i) slot[nodes[i]] = (int)i;
+        T.hlist.insert(T.hlist.end(), nodes.begin(), nodes.end());
+        T.hptr[t + 1] = (int)T.hlist.size();
+        T.hmax = std::max(T.hmax, (int)nodes.size());
+        for (int n = n0; n < n1; ++n) {
+            T.nslot[n] = slot[n];
+            for (int q = P.tptr[n]; q < P.tptr[n + 1]; ++q) {
+                int e = (P.tlist[q] >> 1) >> 2;
+                for (int v = 0; v < 4; ++v) T.tslot[4 * (size_t)q + v] = (unsigned short)slot[P.econn[(size_t)e * 4 + v]];
+            }
+            for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) T.lslot[q] = slot[P.llist[2 * (size_t)q + 1]];
+        }
+        for (int x : nodes) slot[x] = -1;
+    }
+    return EXFEM_OK;
+}
+
 }  // namespace exfem

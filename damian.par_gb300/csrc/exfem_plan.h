@@ -78,6 +78,20 @@ struct Plan {
     std::vector<int> odptr, odlist;
 };
 
+// Shared-memory tiles of the FP32 step: consecutive active nodes (Morton
+// order, so a tile is a compact patch) and the halo of nodes their terms read.
+struct Tiles {
+    int tn = 0;                        // nodes per tile
+    int ntiles = 0;
+    int hmax = 0;                      // largest halo
+    std::vector<int> hptr, hlist;      // halo node ids per tile (sorted)
+    std::vector<unsigned short> tslot; // 4 per gather term: halo slots of the element's corners
+    std::vector<int> nslot;            // per active node: its own halo slot
+    std::vector<int> lslot;            // per anchor link: halo slot of the other anchor
+};
+
+int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err);
+
 // Build the plan.  Returns EXFEM_OK or an EXFEM_E_* code with err filled.
 int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &plan, std::string &err);
 

@@ -1,9 +1,10 @@
-"""Autotuner for the FP32 step kernel's launch shape.
+"""Autotuner for the FP32 step kernel.
 
-Tries (block size, right-hand sides per thread) on the real model: each
-candidate gets its own context, a few warm-up steps and a CUDA-event-timed
-burst on the library's stream; the fastest shape wins.  Results are cached
-per (elements, nodes, rhs) in-process.
+Tries (kernel variant, block size, right-hand sides per thread) on the real
+model — variant 0 is the direct gather, 1 the shared-memory tiled kernel.
+Each candidate gets its own context, a few warm-up steps and a
+CUDA-event-timed burst on the library's stream; the fastest wins.  Results
+are cached per (elements, nodes, rhs) in-process.
 """
 from __future__ import annotations
 
@@ -17,7 +18,7 @@ _cache: dict = {}
 
 def candidates(R):
     rpts = [r for r in (1, 2, 4) if R % r == 0]
-    return [(bt, r) for r in rpts for bt in (128, 256, 512)]
+    return [(v, bt, r) for v in (0, 1) for r in rpts for bt in (128, 256, 512)]
 
 
 def tune(model, steps=12, warmup=3, device=0, verbose=False):
@@ -30,10 +31,10 @@ def tune(model, steps=12, warmup=3, device=0, verbose=False):
     need = warmup + steps
     if model.problem.nsteps < need:
         raise ExfemError(-1, "autotune needs %d steps in the model" % need)
-    for bt, rpt in candidates(R):
+    for var, bt, rpt in candidates(R):
         try:
             s = Solver(model, precision=EXFEM_FP32_KAHAN, device=device, block_threads=bt, rhs_per_thread=rpt,
-                       use_graph=0)
+                       use_graph=0, variant=var)
         except ExfemError:
             continue
         try:
@@ -48,13 +49,15 @@ def tune(model, steps=12, warmup=3, device=0, verbose=False):
             s.close()
         if rc != 0:
             continue
-        results.append((ms.value / steps, bt, rpt))
+        results.append((ms.value / steps, var, bt, rpt))
         if best is None or ms.value < best[0]:
-            best = (ms.value, bt, rpt)
+            best = (ms.value, var, bt, rpt)
     if verbose:
         for r in sorted(results):
-            print("autotune: %.4f ms/step block %d rhs/thread %d" % r)
-    choice = {"block_threads": best[1], "rhs_per_thread": best[2], "ms_per_step": best[0] / steps,
-              "tried": [{"ms_per_step": a, "block_threads": b, "rhs_per_thread": c} for a, b, c in sorted(results)]}
+            print("autotune: %.4f ms/step variant %d block %d rhs/thread %d" % r)
+    choice = {"variant": best[1], "block_threads": best[2], "rhs_per_thread": best[3],
+              "ms_per_step": best[0] / steps,
+              "tried": [{"ms_per_step": a, "variant": v, "block_threads": b, "rhs_per_thread": c}
+                        for a, v, b, c in sorted(results)]}
     _cache[key] = choice
     return choice

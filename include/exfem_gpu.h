@@ -110,8 +110,9 @@ typedef struct exfem_opts {
     int rhs_per_thread;/* right-hand sides per thread in batched form (0 = auto)  */
     int reorder;       /* 1: renumber nodes/elements in Morton order on device    */
     int check_every;   /* non-finite watchdog period in steps (0 = off)           */
-    int variant;       /* FP64 kernels: EXFEM_VARIANT_REFERENCE_ORDER (default)
-                          or EXFEM_VARIANT_CLOSED_FORM                            */
+    int variant;       /* FP64: EXFEM_VARIANT_REFERENCE_ORDER (default) or
+                          EXFEM_VARIANT_CLOSED_FORM.  FP32: 0 = direct gather
+                          (default), 1 = shared-memory tiled step             */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;

@@ -121,6 +121,22 @@ int probe_plan_copy(void *h, const char *name, void *out) {
     return -1;
 }
 
+// Shared-memory tiles of a plan: fills sizes[0..3] = (ntiles, hmax, halo
+// entries, tn) and, when the pointers are non-NULL, copies the arrays.
+int probe_tiles(void *h, int tn, int *sizes, int *hptr, int *hlist, unsigned short *tslot, int *nslot, int *lslot) {
+    Plan &p = *static_cast<Plan *>(h);
+    Tiles T;
+    int rc = build_tiles(p, tn, T, g_err);
+    if (rc) return rc;
+    sizes[0] = T.ntiles; sizes[1] = T.hmax; sizes[2] = (int)T.hlist.size(); sizes[3] = T.tn;
+    if (hptr) std::memcpy(hptr, T.hptr.data(), T.hptr.size() * sizeof(int));
+    if (hlist) std::memcpy(hlist, T.hlist.data(), T.hlist.size() * sizeof(int));
+    if (tslot) std::memcpy(tslot, T.tslot.data(), T.tslot.size() * sizeof(unsigned short));
+    if (nslot) std::memcpy(nslot, T.nslot.data(), T.nslot.size() * sizeof(int));
+    if (lslot && !T.lslot.empty()) std::memcpy(lslot, T.lslot.data(), T.lslot.size() * sizeof(int));
+    return 0;
+}
+
 // Free-field displacement+acceleration at a point for RHS r of a plan
 // (what k_drm evaluates).
 void probe_plan_wave(void *h, int r, double t, double x1, double x3, double *u6) {

@@ -56,6 +56,8 @@ def lib():
     L.probe_plan_size.argtypes = [C.c_void_p, C.c_char_p]
     L.probe_plan_copy.restype = C.c_int
     L.probe_plan_copy.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
+    L.probe_tiles.restype = C.c_int
+    L.probe_tiles.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 5
     L.probe_plan_wave.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, d]
     _lib = L
     return L
@@ -92,6 +94,21 @@ class PlanView:
         out = out[:n]
         self.__dict__[name] = out
         return out
+
+    def tiles(self, tn):
+        """(hptr, hlist, tslot (nterms, 4), nslot, lslot, hmax) of build_tiles."""
+        L = lib()
+        sz = (C.c_int * 4)()
+        assert L.probe_tiles(self.h, tn, sz, None, None, None, None, None) == 0
+        nt, hmax, nh = sz[0], sz[1], sz[2]
+        hptr = np.zeros(nt + 1, np.int32)
+        hlist = np.zeros(max(nh, 1), np.int32)
+        tslot = np.zeros(4 * len(self.tlist), np.uint16)
+        nslot = np.zeros(int(self.scalars[0]), np.int32)
+        lslot = np.zeros(max(len(self.llist) // 2, 1), np.int32)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        assert L.probe_tiles(self.h, tn, sz, vp(hptr), vp(hlist), vp(tslot), vp(nslot), vp(lslot)) == 0
+        return hptr, hlist[:nh], tslot.reshape(-1, 4), nslot, lslot[:len(self.llist) // 2], hmax
 
     def wave(self, r, t, x1, x3):
         out = np.zeros(6)

@@ -113,6 +113,25 @@ def test_plan_gather_lists_cover_every_incidence():
     assert np.array_equal(P.hang.reshape(-1, 3)[:, 0], na + np.arange(nh))
 
 
+@pytest.mark.parametrize("tn", [1, 16, 32, 100])
+def test_tile_halo_slots_point_at_the_right_nodes(tn):
+    m = workloads.build("canyon", scale=0.2, steps=5)
+    P = npb.PlanView(m)
+    na = int(P.scalars[0])
+    hptr, hlist, tslot, nslot, lslot, hmax = P.tiles(tn)
+    econn = P.econn.reshape(-1, 4)
+    assert len(hptr) == (na + tn - 1) // tn + 1 and hmax == np.diff(hptr).max()
+    node_tile = np.arange(na) // tn
+    term_node = np.repeat(np.arange(na), np.diff(P.tptr))
+    base = hptr[node_tile[term_node]]
+    e = (P.tlist >> 1) >> 2
+    assert np.array_equal(hlist[base[:, None] + tslot], econn[e])
+    assert np.array_equal(hlist[hptr[node_tile] + nslot], np.arange(na))
+    link_node = np.repeat(np.arange(na), np.diff(P.lptr))
+    if link_node.size:
+        assert np.array_equal(hlist[hptr[node_tile[link_node]] + lslot], P.llist.reshape(-1, 2)[:, 1])
+
+
 @pytest.mark.parametrize("name,scale,steps,kw", [("homogeneous_rectangle", 0.125, 250, {}),
                                                   ("canyon", 0.15, 500, {"refine_band": 20})])
 def test_kernel_emulation_matches_oracle(name, scale, steps, kw):

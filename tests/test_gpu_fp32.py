@@ -37,20 +37,21 @@ def test_rectangle_fp32_vs_oracle():
     assert peak_rel(g[0], o["seis"]).max() <= TOL
 
 
-def test_canyon_fp32_every_rhs_vs_oracle():
+@pytest.mark.parametrize("variant", [0, 1])
+def test_canyon_fp32_every_rhs_vs_oracle(variant):
     m = workloads.build("canyon", scale=0.15, steps=900, save_every=2, refine_band=20)
-    g, _ = run32(m)
+    g, _ = run32(m, variant=variant)
     for r in range(m.problem.nrhs):
         o = oracle.run(m, rhs=r, nthreads=NT)
         assert np.abs(o["seis"]).max() > 0.1
         assert per_receiver_rel(g[r], o["seis"]).max() <= TOL, r
 
 
-@pytest.mark.parametrize("rpt", [1, 2, 4])
-def test_batched_valley_rhs_match_oracle_for_every_tile(rpt):
+@pytest.mark.parametrize("variant,rpt", [(0, 1), (0, 2), (0, 4), (1, 1), (1, 2), (1, 4)])
+def test_batched_valley_rhs_match_oracle_for_every_kernel_and_tile(variant, rpt):
     m = workloads.build("valley_batched", scale=0.1, steps=500, save_every=5)
     assert m.problem.nrhs == 64
-    g, _ = run32(m, rhs_per_thread=rpt, block_threads=128 * rpt)
+    g, _ = run32(m, rhs_per_thread=rpt, block_threads=128 * rpt, variant=variant)
     for r in (0, 21, 40, 63):
         o = oracle.run(m, rhs=r, nthreads=NT)
         err = per_receiver_rel(g[r], o["seis"])
@@ -106,4 +107,12 @@ def test_autotuner_picks_a_working_shape():
     m = workloads.build("valley_batched", scale=0.1, steps=40)
     choice = autotune.tune(m, steps=8, warmup=2)
     assert choice["rhs_per_thread"] in (1, 2, 4) and choice["block_threads"] in (128, 256, 512)
-    assert len(choice["tried"]) >= 6
+    assert choice["variant"] in (0, 1) and len(choice["tried"]) >= 12
+
+
+def test_tiled_and_direct_kernels_agree():
+    m = workloads.build("canyon", scale=0.2, steps=300, save_every=3)
+    a, _ = run32(m, variant=0)
+    b, _ = run32(m, variant=1)
+    for r in range(m.problem.nrhs):
+        assert per_receiver_rel(a[r], b[r]).max() <= 1e-6
