@@ -131,7 +131,8 @@ def kernel_bytes(name, m, R, fp64):
       k_drm*                read corner coordinates (64 B), write 16 forces*s*R
                             per DRM element
       k_hang*               hanging nodes 3 values in/1 out, receivers
-      k_step32              FP32 increment form, fused: read u_hi, Kahan term
+      k_step32/_tile32/_pipe32
+                            FP32 increment form, fused: read u_hi, Kahan term
                             and increment, write all three (6*ndof*4*R), read
                             element data (conn 16 + coef 16) and lists
     """
@@ -148,7 +149,7 @@ def kernel_bytes(name, m, R, fp64):
         return ns * (64 + 16 * s * R)
     if name.startswith("k_hang"):
         return nh * 2 * 3 * s * R + nr * (4 * 2 * s * R + 2 * 8 * R)
-    if name.startswith("k_step32"):
+    if name.startswith(("k_step32", "k_tile32", "k_pipe32")):
         return 6 * ndof * 4 * R + ne * 32 + 4 * inc
     return None
 

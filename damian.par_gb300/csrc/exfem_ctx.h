@@ -54,6 +54,7 @@ struct DevModel {
     const float *ncoef4;           // per active node: 1/m_full (x, y), -2 a2 C (x, y)
     const float *hcoef4;           // per hanging entry: -2 a2 C (x, y), a1 M + a2 C (x, y)
     float *fdrm32;                 // ns * 8 * R DRM forces (FP64 math, stored FP32)
+    const int *tcorn;              // 4 per gather term: the corners of its element
     // mutable state
     double *fdrm;            // ns * 16 * R DRM forces (stiffness part, mass part)
     double *seis;            // R * nsave * nrecv * 2
@@ -86,6 +87,13 @@ struct Ctx {
     size_t tile_smem = 0;
     const int *t_hptr = nullptr, *t_hlist = nullptr, *t_nslot = nullptr, *t_lslot = nullptr;
     const unsigned short *t_tslot = nullptr;
+    // bulk-copy pipeline of the FP32 step (variant 2): per-tile headers and
+    // halo runs, node records, term records; persistent grid
+    bool use_pipe = false;
+    const void *p_hdr = nullptr, *p_runs = nullptr, *p_nrec = nullptr, *p_tpack = nullptr;
+    int pipe_grid = 0, pipe_threads = 0, pipe_nstage = 0;
+    unsigned pipe_stage = 0;
+    unsigned pipe_off[6] = {0, 0, 0, 0, 0, 0};   // D, D_comp, u_comp, node records, slots, coefficients
     int parity = 0;          // index of the current u buffer
     int steps_done = 0;
     bool inited = false;

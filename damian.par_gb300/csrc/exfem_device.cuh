@@ -51,6 +51,42 @@ __host__ __device__ __forceinline__ void q4_ku_corner(T A, T B, T C, T D, const 
     fy = sP * S + sQ * F2 + sG * Gy;
 }
 
+__host__ __device__ __forceinline__ float q4fma(float a, float b, float c) { return fmaf(a, b, c); }
+__host__ __device__ __forceinline__ double q4fma(double a, double b, double c) { return fma(a, b, c); }
+
+// q4_ku_corner folded for accumulation.  With s = c2x + c1y,
+//   fx = sP A c1x + sP B c2y + sQ C s + sG D c3x
+//   fy = sP C s + sQ A c2y + sQ B c1x + sG D c3y,
+// so one (element, corner, weight w) term of a node's force sum, -w (fx, fy),
+// is 8 multiply-adds on the modes with 7 coefficients scaled by -w and the
+// corner's signs, computed once per term (the FP32 kernels' form).
+template <typename T>
+struct Q4Fold {
+    T a0, a1, a2, a3;   // c1x, c2y, s, c3x (and c3y) into x
+    T b0, b1, b2;       // s, c2y, c1x into y
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ Q4Fold<T> q4_fold(T A, T B, T C, T D, int c, T w) {
+    const T sP = (c == 1 || c == 2) ? -w : w;
+    const T sQ = (c >= 2) ? -w : w;
+    const T sG = (c == 0 || c == 2) ? -w : w;
+    return Q4Fold<T>{sP * A, sP * B, sQ * C, sG * D, sP * C, sQ * A, sQ * B};
+}
+
+// ax += -w fx, ay += -w fy for the folded term f.
+template <typename T>
+__host__ __device__ __forceinline__ void q4_corner_acc(const Q4Fold<T> &f, const T ux[4], const T uy[4], T &ax,
+                                                       T &ay) {
+    T px = ux[2] - ux[0], qx = ux[1] - ux[3];
+    T c1x = px + qx, c2x = px - qx, c3x = (ux[0] + ux[2]) - (ux[1] + ux[3]);
+    T py = uy[2] - uy[0], qy = uy[1] - uy[3];
+    T c1y = py + qy, c2y = py - qy, c3y = (uy[0] + uy[2]) - (uy[1] + uy[3]);
+    T s = c2x + c1y;
+    ax = q4fma(f.a3, c3x, q4fma(f.a2, s, q4fma(f.a1, c2y, q4fma(f.a0, c1x, ax))));
+    ay = q4fma(f.a3, c3y, q4fma(f.b2, c1x, q4fma(f.b1, c2y, q4fma(f.b0, s, ay))));
+}
+
 // Consistent mass (calcsqm/9, formulation.f90:256-268) times v for one
 // component: weights 4 (self), 2 (edge neighbours), 1 (opposite corner).
 template <typename T>

@@ -180,7 +180,10 @@ __global__ void k_drm32(DevModel m) {
     for (int k = 0; k < 8; ++k) m.fdrm32[((size_t)s * 8 + k) * m.R + r] = p[k];
 }
 
-// The fused step for one non-hanging node and RPT right-hand sides.
+// The fused step for one non-hanging node and RPT right-hand sides.  The
+// corners of each term's element come from the per-term copy m.tcorn, loaded
+// beside the term itself (not from econn after it), so the gather chain is
+// term -> corner u_hi.
 template <int RPT>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
@@ -222,14 +225,13 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
     }
     // element terms: -K_e u_e at this node's corner (and its hanging nodes' at 1/2)
-    const int4 *econn4 = reinterpret_cast<const int4 *>(m.econn);
     const float4 *coef4 = reinterpret_cast<const float4 *>(m.ecoef32);
     for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
         int ent = __ldg(m.tlist + q);
+        int4 cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn) + q);
         float w = (ent & 1) ? 0.5f : 1.0f;
         int ec = ent >> 1;
         int e = ec >> 2, c = ec & 3;
-        int4 cn = __ldg(econn4 + e);
         float4 k = __ldg(coef4 + e);
         const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
         float ux[4][RPT], uy[4][RPT];
@@ -239,14 +241,12 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
             Vec<RPT>::load(uh + b, ux[v]);
             Vec<RPT>::load(uh + b + R, uy[v]);
         }
+        const Q4Fold<float> f = q4_fold<float>(k.x, k.y, k.z, k.w, c, w);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
             float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
             float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
-            float fx, fy;
-            q4_ku_corner<float>(k.x, k.y, k.z, k.w, vx, vy, c, fx, fy);
-            ax[j] -= w * fx;
-            ay[j] -= w * fy;
+            q4_corner_acc<float>(f, vx, vy, ax[j], ay[j]);
         }
     }
     // dashpot term -2 a2 C D (zero away from the absorbing boundary)
@@ -394,14 +394,12 @@ __global__ void __launch_bounds__(512) k_tile32(DevModel m, TileArgs ta, const f
             VecS<RPT>::load(sm + ss[v] * row + rl, ux[v]);
             VecS<RPT>::load(sm + ss[v] * row + RC + rl, uy[v]);
         }
+        const Q4Fold<float> f = q4_fold<float>(k.x, k.y, k.z, k.w, c, w);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
             float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
             float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
-            float fx, fy;
-            q4_ku_corner<float>(k.x, k.y, k.z, k.w, vx, vy, c, fx, fy);
-            ax[j] -= w * fx;
-            ay[j] -= w * fy;
+            q4_corner_acc<float>(f, vx, vy, ax[j], ay[j]);
         }
     }
     const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
@@ -460,6 +458,305 @@ __global__ void __launch_bounds__(512) k_tile32(DevModel m, TileArgs ta, const f
     Half<RPT>::store(uc + bn + R, ucy);
     Vec<RPT>::store(uhn + bn, ox);
     Vec<RPT>::store(uhn + bn + R, oy);
+}
+
+// ---- bulk-copy pipeline (variant 2) ----------------------------------------
+//
+// A persistent kernel.  Each block walks tiles t = blockIdx.x, + gridDim.x,
+// ...  A tile is `tn` consecutive active nodes over all R right-hand sides,
+// and everything its update reads lies in a few contiguous runs of HBM:
+//   - the u_hi rows of its halo, merged into runs of consecutive node ids;
+//   - its own D, D_comp and u_comp rows;
+//   - its node records, 32 bytes per node in node order: 1/m_full and
+//     -2 a2 C (float4), then (first term in the tile | terms << 16, halo slot
+//     of the node, DRM start | count << 24, anchor-link start | count << 24);
+//   - its term records, packed per tile: the halo slots of the element's
+//     corners as ushort4 (the node's corner in bits 14-15 of the first) for an
+//     even number of terms, then the element's (A, B, C, D) times the term's
+//     weight as float4 (a power of two: the sums are those of k_step32, bit
+//     for bit).
+// Warp 0 is the producer.  Its lanes issue those runs as cp.async.bulk copies
+// into a shared-memory stage, one halo run per lane; the copies complete on
+// the stage's "full" mbarrier, whose byte count lane 0 sets with
+// arrive.expect_tx.  The other warps are consumers: each thread waits on
+// "full", updates one (node, RPT right-hand sides) from shared memory, stores
+// to HBM from registers, and each warp arrives on the stage's "empty" mbarrier,
+// which the producer waits on before it refills the stage.  With S stages the
+// producer runs S - 1 tiles ahead, and it loads the next tile's header and
+// runs while it issues the current one.  Consumers read HBM only for DRM
+// forces and hanging-node D (boundary-layer and anchor nodes).
+// Every wait is bounded in time.  A warp that times out sets bit 2 of the
+// watchdog flag and leaves; the producer then waits (bounded again) for the
+// copies it issued before it leaves, so no copy outlives its block.
+struct PipeArgs {
+    const int4 *hdr;        // per tile: (halo nodes, terms, term-pack offset in 16 B, runs)
+    const int2 *runs;       // per tile: PIPE_RUNS (first node, count), count 0 past the last
+    const int4 *nrec;       // per active node: 2 int4 (node record)
+    const int4 *tpack;      // term records, per tile
+    const int *lslot;       // per anchor link: halo slot of the other anchor
+    int tn, ntiles, nstage;
+    unsigned stage_bytes;   // one stage; regions at the offsets below
+    unsigned off_dh, off_dc, off_uc, off_nrec, off_ts, off_tk;
+};
+
+constexpr int PIPE_RUNS = 64;
+constexpr int PIPE_MAX_STAGES = 4;
+constexpr long long PIPE_WAIT_CYCLES = 2000000000LL;   // about 1 s at 2 GHz
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+    const long long t0 = clock64();
+    for (int it = 0; it < (1 << 26); ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (clock64() - t0 > PIPE_WAIT_CYCLES) break;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ int warp_excl_scan(int v, int lane, int &total) {
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
+
+// Warp 0 of a k_pipe32 block: issues every tile's copies.
+__device__ __forceinline__ void pipe_produce(const DevModel &m, const PipeArgs &pa, unsigned char *stage0,
+                                             unsigned long long *full, unsigned long long *empty,
+                                             const float *uh, const float *dh, const unsigned short *dc,
+                                             const unsigned short *uc) {
+    const int lane = threadIdx.x & 31;
+    const unsigned R = (unsigned)m.R;
+    const int NS = pa.nstage;
+    int t = blockIdx.x;
+    if (t >= pa.ntiles) return;
+    int4 h = __ldg(pa.hdr + t);
+    int2 ra = __ldg(pa.runs + (size_t)t * PIPE_RUNS + lane);
+    int2 rb = __ldg(pa.runs + (size_t)t * PIPE_RUNS + 32 + lane);
+    int k = 0;
+    bool ok = true;
+    for (; t < pa.ntiles; t += gridDim.x, ++k) {
+        // the next tile's header and runs load while this one is issued
+        const int tnext = t + gridDim.x;
+        int4 h2 = h;
+        int2 ra2 = ra, rb2 = rb;
+        if (tnext < pa.ntiles) {
+            h2 = __ldg(pa.hdr + tnext);
+            ra2 = __ldg(pa.runs + (size_t)tnext * PIPE_RUNS + lane);
+            rb2 = __ldg(pa.runs + (size_t)tnext * PIPE_RUNS + 32 + lane);
+        }
+        const int s = k % NS;
+        if (k >= NS) {
+            const bool w = mbar_wait_bounded(smem_addr(empty + s), (unsigned)(k / NS - 1) & 1u);
+            if (!__all_sync(0xffffffffu, w)) { ok = false; break; }
+            // the consumers' reads of the stage (generic proxy) come before the refill (async proxy)
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        int tota, totb;
+        const int offa = warp_excl_scan(ra.y, lane, tota);
+        const int offb = tota + warp_excl_scan(rb.y, lane, totb);
+        const unsigned base = smem_addr(stage0 + (size_t)s * pa.stage_bytes);
+        const unsigned bar = smem_addr(full + s);
+        const int n0 = t * pa.tn;
+        const unsigned cnt = (unsigned)min(pa.tn, m.n_active - n0);
+        const unsigned nt = (unsigned)h.y, ntev = (nt + 1u) & ~1u;
+        if (lane == 0) {
+            const unsigned bytes = (unsigned)h.x * 8u * R + cnt * (16u * R + 32u) + ntev * 8u + nt * 16u;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+        }
+        __syncwarp();
+        if (ra.y > 0) bulk_g2s(base + (unsigned)offa * 8u * R, uh + (size_t)ra.x * 2 * R, (unsigned)ra.y * 8u * R, bar);
+        if (rb.y > 0) bulk_g2s(base + (unsigned)offb * 8u * R, uh + (size_t)rb.x * 2 * R, (unsigned)rb.y * 8u * R, bar);
+        const size_t o = (size_t)n0 * 2 * R;
+        if (lane == 0) bulk_g2s(base + pa.off_dh, dh + o, cnt * 8u * R, bar);
+        if (lane == 1) bulk_g2s(base + pa.off_dc, dc + o, cnt * 4u * R, bar);
+        if (lane == 2) bulk_g2s(base + pa.off_uc, uc + o, cnt * 4u * R, bar);
+        if (lane == 3) bulk_g2s(base + pa.off_nrec, pa.nrec + 2 * (size_t)n0, cnt * 32u, bar);
+        if (lane == 4 && nt > 0) bulk_g2s(base + pa.off_ts, pa.tpack + h.z, ntev * 8u, bar);
+        if (lane == 5 && nt > 0) bulk_g2s(base + pa.off_tk, pa.tpack + h.z + ntev / 2, nt * 16u, bar);
+        h = h2;
+        ra = ra2;
+        rb = rb2;
+    }
+    if (!ok) {
+        if (lane == 0) {
+            atomicOr(m.d_flag, 2);
+            for (int j = max(0, k - NS); j < k; ++j)   // copies that may still be in flight
+                mbar_wait_bounded(smem_addr(full + j % NS), (unsigned)(j / NS) & 1u);
+        }
+    }
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(544) k_pipe32(DevModel m, PipeArgs pa, const float *__restrict__ uh,
+                                                float *__restrict__ uhn, unsigned short *__restrict__ uc,
+                                                float *__restrict__ dh, unsigned short *__restrict__ dc) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    // [0, 64): full mbarriers, [64, 128): empty mbarriers; stages from byte 128
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(smraw);
+    unsigned long long *empty = full + PIPE_MAX_STAGES;
+    unsigned char *stage0 = smraw + 128;
+    const int NS = pa.nstage;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        const unsigned ncons = (blockDim.x >> 5) - 1;
+        for (int s = 0; s < NS; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(full + s)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(empty + s)), "r"(ncons));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        pipe_produce(m, pa, stage0, full, empty, uh, dh, dc, uc);
+        return;
+    }
+    const int R = m.R, G = R / RPT, row = 2 * R;
+    const int ct = threadIdx.x - 32;
+    const int ln = ct / G, g = ct - ln * G;
+    const int rl = g * RPT, r0 = rl;
+    int k = 0;
+    for (int t = blockIdx.x; t < pa.ntiles; t += gridDim.x, ++k) {
+        const int s = k % NS;
+        const bool w = mbar_wait_bounded(smem_addr(full + s), (unsigned)(k / NS) & 1u);
+        if (!__all_sync(0xffffffffu, w)) {
+            if (lane == 0) atomicOr(m.d_flag, 2);
+            return;
+        }
+        const unsigned char *st = stage0 + (size_t)s * pa.stage_bytes;
+        const float *sh = reinterpret_cast<const float *>(st);
+        const int n = t * pa.tn + ln;
+        if (ln < pa.tn && n < m.n_active) {
+            const size_t bn = ((size_t)n * 2) * R + r0;
+            const int so = ln * row + rl;   // own row offset in the D region
+            const float *sd = reinterpret_cast<const float *>(st + pa.off_dh);
+            const unsigned short *sdc = reinterpret_cast<const unsigned short *>(st + pa.off_dc);
+            const unsigned short *suc = reinterpret_cast<const unsigned short *>(st + pa.off_uc);
+            const int4 *snr = reinterpret_cast<const int4 *>(st + pa.off_nrec);
+            const uint2 *sts = reinterpret_cast<const uint2 *>(st + pa.off_ts);
+            const float4 *stk = reinterpret_cast<const float4 *>(st + pa.off_tk);
+            const int4 meta = snr[2 * ln + 1];
+            const int tb = meta.x & 0xffff, tc = (int)((unsigned)meta.x >> 16);
+            const int dbeg = meta.z & 0xffffff, dcnt = (int)((unsigned)meta.z >> 24);
+            const int lbeg = meta.w & 0xffffff, lcnt = (int)((unsigned)meta.w >> 24);
+            float ax[RPT], ay[RPT];
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) { ax[j] = 0.f; ay[j] = 0.f; }
+            for (int q = dbeg; q < dbeg + dcnt; ++q) {
+                int ent = __ldg(m.dlist + q);
+                float w = (ent & 1) ? 0.5f : 1.0f;
+                int sc = ent >> 1;
+                size_t b = ((size_t)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
+                float fx[RPT], fy[RPT];
+                Vec<RPT>::load_cg(m.fdrm32 + b, fx);
+                Vec<RPT>::load_cg(m.fdrm32 + b + R, fy);
+#pragma unroll
+                for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
+            }
+            for (int q = tb; q < tb + tc; ++q) {
+                const uint2 sl = sts[q];
+                const float4 kc = stk[q];
+                const int c = (int)((sl.x >> 14) & 3u);
+                const int ss[4] = {(int)(sl.x & 0x3fffu), (int)(sl.x >> 16), (int)(sl.y & 0xffffu), (int)(sl.y >> 16)};
+                float ux[4][RPT], uy[4][RPT];
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    VecS<RPT>::load(sh + ss[v] * row + rl, ux[v]);
+                    VecS<RPT>::load(sh + ss[v] * row + R + rl, uy[v]);
+                }
+                const Q4Fold<float> f = q4_fold<float>(kc.x, kc.y, kc.z, kc.w, c, 1.0f);
+#pragma unroll
+                for (int j = 0; j < RPT; ++j) {
+                    float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
+                    float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
+                    q4_corner_acc<float>(f, vx, vy, ax[j], ay[j]);
+                }
+            }
+            const int4 nci = snr[2 * ln];
+            const float4 nc = make_float4(__int_as_float(nci.x), __int_as_float(nci.y), __int_as_float(nci.z),
+                                          __int_as_float(nci.w));
+            float dx[RPT], dy[RPT];
+            VecS<RPT>::load(sd + so, dx);
+            VecS<RPT>::load(sd + so + R, dy);
+            if (nc.z != 0.f || nc.w != 0.f) {
+#pragma unroll
+                for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
+            }
+            float unx[RPT], uny[RPT];
+            VecS<RPT>::load(sh + meta.y * row + rl, unx);
+            VecS<RPT>::load(sh + meta.y * row + R + rl, uny);
+            for (int q = lbeg; q < lbeg + lcnt; ++q) {
+                int hn = __ldg(m.llist + 2 * q);
+                int sb = __ldg(pa.lslot + q);
+                float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (hn - m.n_active));
+                size_t bh = ((size_t)hn * 2) * R + r0;
+                float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
+                Vec<RPT>::load_cg(dh + bh, hx);
+                Vec<RPT>::load_cg(dh + bh + R, hy);
+                VecS<RPT>::load(sh + sb * row + rl, ubx);
+                VecS<RPT>::load(sh + sb * row + R + rl, uby);
+#pragma unroll
+                for (int j = 0; j < RPT; ++j) {
+                    ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j]) + (hx[j] - dx[j])));
+                    ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j]) + (hy[j] - dy[j])));
+                }
+            }
+            float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
+            Half<RPT>::load(sdc + so, dcx);
+            Half<RPT>::load(sdc + so + R, dcy);
+            Half<RPT>::load(suc + so, ucx);
+            Half<RPT>::load(suc + so + R, ucy);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) {
+                float yx = ax[j] * nc.x - dcx[j], yy = ay[j] * nc.y - dcy[j];
+                float tx = dx[j] + yx, ty = dy[j] + yy;
+                dcx[j] = (tx - dx[j]) - yx;
+                dcy[j] = (ty - dy[j]) - yy;
+                dx[j] = tx;
+                dy[j] = ty;
+                float vx = tx - ucx[j], vy = ty - ucy[j];
+                float sx = unx[j] + vx, sy = uny[j] + vy;
+                ucx[j] = (sx - unx[j]) - vx;
+                ucy[j] = (sy - uny[j]) - vy;
+                ox[j] = sx;
+                oy[j] = sy;
+            }
+            Vec<RPT>::store(dh + bn, dx);
+            Vec<RPT>::store(dh + bn + R, dy);
+            Half<RPT>::store(dc + bn, dcx);
+            Half<RPT>::store(dc + bn + R, dcy);
+            Half<RPT>::store(uc + bn, ucx);
+            Half<RPT>::store(uc + bn + R, ucy);
+            Vec<RPT>::store(uhn + bn, ox);
+            Vec<RPT>::store(uhn + bn + R, oy);
+        }
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(empty + s)) : "memory");
+    }
 }
 
 // u of one node in FP64 (u_hi - comp); hanging corners read as anchor averages.
@@ -581,17 +878,86 @@ static int pick_rpt(const Ctx &c) {
     return 1;
 }
 
+// Tiles, their headers and halo runs, node and term records for k_pipe32,
+// and the stage layout.  Leaves c.use_pipe false when the model does not fit
+// the record formats or shared memory.
+static int pipe_setup(Ctx &c) {
+    const Plan &P = c.plan;
+    const int R = P.R, rpt = c.rhs_per_thread, G = R / rpt;
+    const int tn = c.block_threads / G;
+    if (tn < 1) return EXFEM_OK;
+    const int consumers = (tn * G + 31) / 32 * 32;
+    if (consumers > 512) return EXFEM_OK;
+    Tiles T;
+    std::string terr;
+    if (build_tiles(P, tn, T, terr) != EXFEM_OK) return EXFEM_OK;
+    PipePack pk;
+    if (!build_pipe_pack(P, T, PIPE_RUNS, pk, terr)) return EXFEM_OK;
+    const int tmax = pk.tmax;
+    // stage: halo rows | D | D_comp | u_comp | node records | slots | coefficients
+    const unsigned Ru = (unsigned)R, tnu = (unsigned)tn;
+    const unsigned tmev = (unsigned)((tmax + 1) & ~1);
+    unsigned off[6];
+    off[0] = (unsigned)T.hmax * 8u * Ru;
+    off[1] = off[0] + tnu * 8u * Ru;
+    off[2] = off[1] + tnu * 4u * Ru;
+    off[3] = off[2] + tnu * 4u * Ru;
+    off[4] = off[3] + tnu * 32u;
+    off[5] = off[4] + (tmev * 8u + 15u) / 16u * 16u;
+    const unsigned stage = (off[5] + (unsigned)tmax * 16u + 127u) / 128u * 128u;
+    int dev_smem = 0, nsm = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device);
+    int ns = 0;
+    for (int k = PIPE_MAX_STAGES; k >= 2 && !ns; --k)
+        if (128 + (size_t)k * stage <= (size_t)dev_smem) ns = k;
+    if (!ns || stage >= (1u << 20)) return EXFEM_OK;
+    const size_t smem = 128 + (size_t)ns * stage;
+    const int threads = 32 + consumers;
+    int per_sm = 0, rc;
+    switch (rpt) {
+        case 4:
+            CK(cudaFuncSetAttribute(k_pipe32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pipe32<4>, threads, smem));
+            break;
+        case 2:
+            CK(cudaFuncSetAttribute(k_pipe32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pipe32<2>, threads, smem));
+            break;
+        default:
+            CK(cudaFuncSetAttribute(k_pipe32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pipe32<1>, threads, smem));
+            break;
+    }
+    if (per_sm < 1) return EXFEM_OK;
+    const int *d = nullptr;
+    if ((rc = upload32(c, pk.hdr, &d))) return rc;
+    c.p_hdr = d;
+    if ((rc = upload32(c, pk.runs, &d))) return rc;
+    c.p_runs = d;
+    if ((rc = upload32(c, pk.nrec, &d))) return rc;
+    c.p_nrec = d;
+    if ((rc = upload32(c, pk.tpack, &d))) return rc;
+    c.p_tpack = d;
+    if (!T.lslot.empty() && (rc = upload32(c, T.lslot, &c.t_lslot))) return rc;
+    c.tile_tn = tn;
+    c.tile_n = T.ntiles;
+    c.tile_hmax = T.hmax;
+    c.tile_smem = smem;
+    c.pipe_stage = stage;
+    c.pipe_nstage = ns;
+    c.pipe_threads = threads;
+    for (int k = 0; k < 6; ++k) c.pipe_off[k] = off[k];
+    c.pipe_grid = std::min(T.ntiles, per_sm * std::max(nsm, 1));
+    c.use_pipe = true;
+    return EXFEM_OK;
+}
+
 int f32_alloc(Ctx &c) {
     const Plan &P = c.plan;
     DevModel &m = c.dm;
     // per active node: 1/m_full (x, y), -2 a2 C (x, y)
-    std::vector<float> nc((size_t)4 * P.n_active);
-    for (int n = 0; n < P.n_active; ++n) {
-        nc[4 * (size_t)n] = (float)P.inv_mfull[2 * (size_t)n];
-        nc[4 * (size_t)n + 1] = (float)P.inv_mfull[2 * (size_t)n + 1];
-        nc[4 * (size_t)n + 2] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)n]);
-        nc[4 * (size_t)n + 3] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)n + 1]);
-    }
+    const std::vector<float> nc = node_coef32(P);
     std::vector<float> hc((size_t)4 * std::max(P.n_hang, 1), 0.f);
     for (int i = 0; i < P.n_hang; ++i) {
         int h = P.hang[3 * (size_t)i];
@@ -647,6 +1013,22 @@ int f32_alloc(Ctx &c) {
             }
         }
     }
+    // bulk-copy pipeline (variant 2): needs 16-byte rows (R a multiple of 4)
+    // and at least two stages in shared memory; otherwise the direct gather runs
+    c.use_pipe = false;
+    if (c.opts.variant == 2 && P.R % 4 == 0) {
+        if ((rc = pipe_setup(c))) return rc;
+    }
+    // the direct gather's per-term corner copies
+    m.tcorn = nullptr;
+    if (!c.use_tiles && !c.use_pipe) {
+        std::vector<int> tc(4 * std::max<size_t>(P.tlist.size(), 1), 0);
+        for (size_t q = 0; q < P.tlist.size(); ++q) {
+            const int e = (P.tlist[q] >> 1) >> 2;
+            for (int v = 0; v < 4; ++v) tc[4 * q + v] = P.econn[(size_t)e * 4 + v];
+        }
+        if ((rc = upload32(c, tc, &m.tcorn))) return rc;
+    }
     return EXFEM_OK;
 }
 
@@ -671,7 +1053,20 @@ int f32_launch_step(Ctx &c, int par) {
     const int T = c.block_threads;
     const int rpt = c.rhs_per_thread;
     long long work = (long long)m.n_active * (m.R / rpt);
-    if (c.use_tiles) {
+    if (c.use_pipe) {
+        PipeArgs pa{static_cast<const int4 *>(c.p_hdr), static_cast<const int2 *>(c.p_runs),
+                    static_cast<const int4 *>(c.p_nrec), static_cast<const int4 *>(c.p_tpack), c.t_lslot,
+                    c.tile_tn, c.tile_n, c.pipe_nstage, c.pipe_stage,
+                    c.pipe_off[0], c.pipe_off[1], c.pipe_off[2], c.pipe_off[3], c.pipe_off[4], c.pipe_off[5]};
+        const int threads = c.pipe_threads;
+        switch (rpt) {
+            case 4: k_pipe32<4><<<c.pipe_grid, threads, c.tile_smem, c.stream>>>(m, pa, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            case 2: k_pipe32<2><<<c.pipe_grid, threads, c.tile_smem, c.stream>>>(m, pa, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            default: k_pipe32<1><<<c.pipe_grid, threads, c.tile_smem, c.stream>>>(m, pa, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        }
+        c.launches++;
+        mark(c, "k_pipe32");
+    } else if (c.use_tiles) {
         TileArgs ta{c.t_hptr, c.t_hlist, c.t_nslot, c.t_lslot, c.t_tslot, c.tile_tn, c.tile_rc};
         dim3 grid(c.tile_n, m.R / c.tile_rc);
         int threads = c.tile_tn * (c.tile_rc / rpt);
@@ -683,10 +1078,11 @@ int f32_launch_step(Ctx &c, int par) {
         c.launches++;
         mark(c, "k_tile32");
     } else {
+    const int nb = nblocks(work, T);
     switch (rpt) {
-        case 4: k_step32<4><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-        case 2: k_step32<2><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-        default: k_step32<1><<<nblocks(work, T), T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        case 4: k_step32<4><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        case 2: k_step32<2><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        default: k_step32<1><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
     }
     c.launches++;
     mark(c, "k_step32");

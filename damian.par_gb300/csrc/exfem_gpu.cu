@@ -384,7 +384,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     if (opts) o = *opts;
     else exfem_gpu_default_opts(&o);
     if (o.precision != EXFEM_FP64 && o.precision != EXFEM_FP32_KAHAN) { g_create_err = "unknown precision"; return EXFEM_E_ARG; }
-    if (o.variant < 0 || o.variant > 1) {
+    if (o.variant < 0 || o.variant > (o.precision == EXFEM_FP32_KAHAN ? 2 : 1)) {
         g_create_err = "unknown kernel variant";
         return EXFEM_E_ARG;
     }
@@ -650,6 +650,12 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
     if (f64) b += R * (nn * 32 + ne * 64);                          // u ping-pong, element forces
     else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 32 * std::max(ns, (size_t)1) * R +
               R * nn * 2 * (4 + 4 + 2 + 4 + 2);                     // FP32 state
+    if (!f64 && opts->variant >= 1) {
+        // tiles: every halo entry is a node or a corner/anchor of one of its terms
+        const size_t H = nn + 16 * (ne + nh) + nh;
+        b += 8 * (nn + 2) + 12 * H + 8 * (4 * ne + 4 * nh) + 4 * nn + 4 * nh;
+    }
+    if (!f64) b += 16 * (4 * ne + 4 * nh);   // per-term corners of the direct gather
     return b + 64 * 1024;
 }
 

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 
 namespace exfem {
@@ -442,6 +443,7 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
     T.tn = tn;
     T.ntiles = (P.n_active + tn - 1) / tn;
     T.hptr.assign(T.ntiles + 1, 0);
+    T.rptr.assign(T.ntiles + 1, 0);
     T.tslot.assign(4 * P.tlist.size(), 0);
     T.nslot.assign(P.n_active, 0);
     T.lslot.assign(P.llist.size() / 2, 0);
@@ -463,6 +465,14 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
         for (size_t i = 0; i < nodes.size(); ++i) slot[nodes[i]] = (int)i;
         T.hlist.insert(T.hlist.end(), nodes.begin(), nodes.end());
         T.hptr[t + 1] = (int)T.hlist.size();
+        for (size_t i = 0; i < nodes.size();) {
+            size_t j = i + 1;
+            while (j < nodes.size() && nodes[j] == nodes[j - 1] + 1) ++j;
+            T.runs.push_back(nodes[i]);
+            T.runs.push_back((int)(j - i));
+            i = j;
+        }
+        T.rptr[t + 1] = (int)(T.runs.size() / 2);
         T.hmax = std::max(T.hmax, (int)nodes.size());
         for (int n = n0; n < n1; ++n) {
             T.nslot[n] = slot[n];
@@ -475,6 +485,68 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
         for (int x : nodes) slot[x] = -1;
     }
     return EXFEM_OK;
+}
+
+std::vector<float> node_coef32(const Plan &P) {
+    std::vector<float> nc((size_t)4 * P.n_active);
+    for (int n = 0; n < P.n_active; ++n) {
+        nc[4 * (size_t)n] = (float)P.inv_mfull[2 * (size_t)n];
+        nc[4 * (size_t)n + 1] = (float)P.inv_mfull[2 * (size_t)n + 1];
+        nc[4 * (size_t)n + 2] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)n]);
+        nc[4 * (size_t)n + 3] = (float)(-2.0 * P.a2 * P.ndamp[2 * (size_t)n + 1]);
+    }
+    return nc;
+}
+
+bool build_pipe_pack(const Plan &P, const Tiles &T, int max_runs, PipePack &out, std::string &why) {
+    out = PipePack();
+    if (T.hmax >= (1 << 14)) { why = "tile halo over 16383 nodes"; return false; }
+    if (P.dlist.size() >= (1u << 24) || P.llist.size() / 2 >= (1u << 24)) { why = "DRM or link list over 2^24"; return false; }
+    auto fbits = [](float f) { int i; std::memcpy(&i, &f, sizeof(i)); return i; };
+    const std::vector<float> nc = node_coef32(P);
+    const int tn = T.tn;
+    out.hdr.assign(4 * (size_t)T.ntiles, 0);
+    out.runs.assign(2 * (size_t)max_runs * T.ntiles, 0);
+    out.nrec.assign(8 * (size_t)P.n_active, 0);
+    for (int t = 0; t < T.ntiles; ++t) {
+        const int n0 = t * tn, n1 = std::min(P.n_active, n0 + tn);
+        const int nr = T.rptr[t + 1] - T.rptr[t];
+        const int q0 = P.tptr[n0], q1 = P.tptr[n1], nt = q1 - q0, ntev = (nt + 1) & ~1;
+        if (nr > max_runs) { why = "tile halo in more than " + std::to_string(max_runs) + " runs"; return false; }
+        if (nt >= (1 << 16)) { why = "tile with 65536 terms or more"; return false; }
+        out.tmax = std::max(out.tmax, nt);
+        int *h = &out.hdr[4 * (size_t)t];
+        h[0] = T.hptr[t + 1] - T.hptr[t];
+        h[1] = nt;
+        h[2] = (int)(out.tpack.size() / 4);
+        h[3] = nr;
+        for (int i = 0; i < 2 * nr; ++i) out.runs[2 * (size_t)t * max_runs + i] = T.runs[2 * (size_t)T.rptr[t] + i];
+        const size_t base = out.tpack.size();
+        out.tpack.resize(base + 2 * (size_t)ntev + 4 * (size_t)nt, 0);
+        for (int q = q0; q < q1; ++q) {
+            const int ent = P.tlist[q], cor = (ent >> 1) & 3, e = (ent >> 1) >> 2;
+            const float w = (ent & 1) ? 0.5f : 1.0f;
+            const unsigned short *sl = &T.tslot[4 * (size_t)q];
+            const unsigned s0 = (unsigned)sl[0] | ((unsigned)cor << 14);
+            out.tpack[base + 2 * (size_t)(q - q0)] = (int)(s0 | ((unsigned)sl[1] << 16));
+            out.tpack[base + 2 * (size_t)(q - q0) + 1] = (int)((unsigned)sl[2] | ((unsigned)sl[3] << 16));
+            for (int v = 0; v < 4; ++v)
+                out.tpack[base + 2 * (size_t)ntev + 4 * (size_t)(q - q0) + v] = fbits(P.ecoef32[(size_t)e * 4 + v] * w);
+        }
+        for (int n = n0; n < n1; ++n) {
+            int *r = &out.nrec[8 * (size_t)n];
+            for (int v = 0; v < 4; ++v) r[v] = fbits(nc[4 * (size_t)n + v]);
+            const int tb = P.tptr[n] - q0, tc = P.tptr[n + 1] - P.tptr[n];
+            const int dcnt = P.dptr[n + 1] - P.dptr[n], lcnt = P.lptr[n + 1] - P.lptr[n];
+            if (dcnt > 255 || lcnt > 255) { why = "node with over 255 DRM terms or links"; return false; }
+            r[4] = (int)((unsigned)tb | ((unsigned)tc << 16));
+            r[5] = T.nslot[n];
+            r[6] = (int)((unsigned)P.dptr[n] | ((unsigned)dcnt << 24));
+            r[7] = (int)((unsigned)P.lptr[n] | ((unsigned)lcnt << 24));
+        }
+    }
+    if (out.tpack.empty()) out.tpack.assign(4, 0);
+    return true;
 }
 
 }  // namespace exfem

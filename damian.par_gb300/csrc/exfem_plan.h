@@ -88,9 +88,34 @@ struct Tiles {
     std::vector<unsigned short> tslot; // 4 per gather term: halo slots of the element's corners
     std::vector<int> nslot;            // per active node: its own halo slot
     std::vector<int> lslot;            // per anchor link: halo slot of the other anchor
+    // runs of consecutive node ids in each tile's sorted halo (for bulk copies)
+    std::vector<int> rptr;             // ntiles + 1
+    std::vector<int> runs;             // (first node, count) pairs
 };
 
 int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err);
+
+// Per active node, the FP32 step's node coefficients: 1/m_full (x, y) and
+// -2 a2 C (x, y).
+std::vector<float> node_coef32(const Plan &P);
+
+// What the bulk-copy pipeline reads per tile, in the formats its kernel
+// decodes (all arrays of 32-bit words, every tile's part 16-byte aligned):
+//   hdr    4 per tile: halo nodes, terms, term-pack offset (16-byte units), runs
+//   runs   2 * max_runs per tile: (first node, count), count 0 past the last
+//   nrec   8 per active node: 1/m_full x, y and -2 a2 C x, y (float bits);
+//          first term in the tile | terms << 16; halo slot of the node;
+//          DRM start | count << 24; anchor-link start | count << 24
+//   tpack  per tile: the halo slots of each term's element corners as
+//          ushort4 (the node's corner in bits 14-15 of the first slot), an
+//          even number of them, then each term's (A, B, C, D) times its
+//          weight (1 or 1/2) as float bits
+// Returns false (with why) when the model exceeds a field of these formats.
+struct PipePack {
+    std::vector<int> hdr, runs, nrec, tpack;
+    int tmax = 0;                      // most terms in a tile
+};
+bool build_pipe_pack(const Plan &P, const Tiles &T, int max_runs, PipePack &out, std::string &why);
 
 // Build the plan.  Returns EXFEM_OK or an EXFEM_E_* code with err filled.
 int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &plan, std::string &err);

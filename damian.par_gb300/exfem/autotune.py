@@ -1,7 +1,8 @@
 """Autotuner for the FP32 step kernel.
 
 Tries (kernel variant, block size, right-hand sides per thread) on the real
-model — variant 0 is the direct gather, 1 the shared-memory tiled kernel.
+model — variant 0 is the direct gather, 1 the shared-memory tiled kernel,
+2 the persistent kernel fed by bulk copies (needs nrhs a multiple of 4).
 Each candidate gets its own context, a few warm-up steps and a
 CUDA-event-timed burst on the library's stream; the fastest wins.  Results
 are cached per (elements, nodes, rhs) in-process.
@@ -18,7 +19,8 @@ _cache: dict = {}
 
 def candidates(R):
     rpts = [r for r in (1, 2, 4) if R % r == 0]
-    return [(v, bt, r) for v in (0, 1) for r in rpts for bt in (128, 256, 512)]
+    vs = (0, 1, 2) if R % 4 == 0 else (0, 1)
+    return [(v, bt, r) for v in vs for r in rpts for bt in (128, 256, 512)]
 
 
 def tune(model, steps=12, warmup=3, device=0, verbose=False):

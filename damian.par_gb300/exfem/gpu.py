@@ -91,6 +91,16 @@ class Solver:
     def device_bytes(self):
         return self.lib.exfem_gpu_device_bytes(self.h)
 
+    def kernel_times(self, steps):
+        """{kernel name: mean ms per launch} over `steps` steps run without a
+        graph (CUDA events between launches on the context's stream)."""
+        ms = (C.c_double * 16)()
+        nm = (C.c_char_p * 16)()
+        nk = self.lib.exfem_gpu_profile_kernels(self.h, int(steps), ms, nm, 16)
+        if nk < 0:
+            self._check(nk)
+        return {nm[i].decode(): ms[i] for i in range(nk)}
+
     def u(self, rhs=0):
         out = np.zeros(2 * self.model.nnodes)
         self._check(self.lib.exfem_gpu_get_u(self.h, int(rhs), _dp(out), out.size))

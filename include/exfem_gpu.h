@@ -112,7 +112,10 @@ typedef struct exfem_opts {
     int check_every;   /* non-finite watchdog period in steps (0 = off)           */
     int variant;       /* FP64: EXFEM_VARIANT_REFERENCE_ORDER (default) or
                           EXFEM_VARIANT_CLOSED_FORM.  FP32: 0 = direct gather
-                          (default), 1 = shared-memory tiled step             */
+                          (default), 1 = shared-memory tiled step, 2 = tiles
+                          streamed by bulk copies through a two-stage
+                          shared-memory pipeline (persistent grid; needs nrhs
+                          a multiple of 4, else the direct gather runs)       */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;

@@ -38,6 +38,15 @@ void probe_q4_ku_corner(double A, double B, double C, double D, const double *ux
     q4_ku_corner<double>(A, B, C, D, ux, uy, c, *fx, *fy);
 }
 
+// -w times the corner force, through q4_fold + q4_corner_acc (from zero).
+void probe_q4_corner_acc(double A, double B, double C, double D, const double *ux, const double *uy, int c, double w,
+                         double *ax, double *ay) {
+    const Q4Fold<double> f = q4_fold<double>(A, B, C, D, c, w);
+    *ax = 0.0;
+    *ay = 0.0;
+    q4_corner_acc<double>(f, ux, uy, *ax, *ay);
+}
+
 void probe_q4_ku_f32(float A, float B, float C, float D, const float *ux, const float *uy, float *fx, float *fy) {
     q4_ku<float>(A, B, C, D, ux, uy, fx, fy);
 }
@@ -134,6 +143,37 @@ int probe_tiles(void *h, int tn, int *sizes, int *hptr, int *hlist, unsigned sho
     if (tslot) std::memcpy(tslot, T.tslot.data(), T.tslot.size() * sizeof(unsigned short));
     if (nslot) std::memcpy(nslot, T.nslot.data(), T.nslot.size() * sizeof(int));
     if (lslot && !T.lslot.empty()) std::memcpy(lslot, T.lslot.data(), T.lslot.size() * sizeof(int));
+    return 0;
+}
+
+// Halo runs of the tiles (the bulk copies of the pipelined step): fills
+// rptr[ntiles + 1] and runs[2 * nruns] when non-NULL; returns nruns.
+int probe_tile_runs(void *h, int tn, int *rptr, int *runs) {
+    Plan &p = *static_cast<Plan *>(h);
+    Tiles T;
+    int rc = build_tiles(p, tn, T, g_err);
+    if (rc) return rc;
+    if (rptr) std::memcpy(rptr, T.rptr.data(), T.rptr.size() * sizeof(int));
+    if (runs) std::memcpy(runs, T.runs.data(), T.runs.size() * sizeof(int));
+    return (int)(T.runs.size() / 2);
+}
+
+// The bulk-copy pipeline's records (build_pipe_pack): sizes[0..4] = (hdr,
+// runs, nrec, tpack words, tmax); the arrays are copied when non-NULL.
+// Returns 0, or 1 when the model does not fit the formats.
+int probe_pipe_pack(void *h, int tn, int max_runs, int *sizes, int *hdr, int *runs, int *nrec, int *tpack) {
+    Plan &p = *static_cast<Plan *>(h);
+    Tiles T;
+    int rc = build_tiles(p, tn, T, g_err);
+    if (rc) return rc;
+    PipePack pk;
+    if (!build_pipe_pack(p, T, max_runs, pk, g_err)) return 1;
+    sizes[0] = (int)pk.hdr.size(); sizes[1] = (int)pk.runs.size(); sizes[2] = (int)pk.nrec.size();
+    sizes[3] = (int)pk.tpack.size(); sizes[4] = pk.tmax;
+    if (hdr) std::memcpy(hdr, pk.hdr.data(), pk.hdr.size() * sizeof(int));
+    if (runs) std::memcpy(runs, pk.runs.data(), pk.runs.size() * sizeof(int));
+    if (nrec) std::memcpy(nrec, pk.nrec.data(), pk.nrec.size() * sizeof(int));
+    if (tpack) std::memcpy(tpack, pk.tpack.data(), pk.tpack.size() * sizeof(int));
     return 0;
 }
 

@@ -40,6 +40,7 @@ def lib():
     L.probe_error.restype = C.c_char_p
     L.probe_q4_ku.argtypes = [C.c_double] * 4 + [d] * 4
     L.probe_q4_ku_corner.argtypes = [C.c_double] * 4 + [d, d, C.c_int, d, d]
+    L.probe_q4_corner_acc.argtypes = [C.c_double] * 4 + [d, d, C.c_int, C.c_double, d, d]
     f = C.POINTER(C.c_float)
     L.probe_q4_ku_f32.argtypes = [C.c_float] * 4 + [f] * 4
     L.probe_drm_forces.argtypes = [d, C.c_double, C.c_int, d, d, d]
@@ -58,6 +59,10 @@ def lib():
     L.probe_plan_copy.argtypes = [C.c_void_p, C.c_char_p, C.c_void_p]
     L.probe_tiles.restype = C.c_int
     L.probe_tiles.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 5
+    L.probe_tile_runs.restype = C.c_int
+    L.probe_pipe_pack.restype = C.c_int
+    L.probe_pipe_pack.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 4
+    L.probe_tile_runs.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     L.probe_plan_wave.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, d]
     _lib = L
     return L
@@ -109,6 +114,33 @@ class PlanView:
         vp = lambda a: a.ctypes.data_as(C.c_void_p)
         assert L.probe_tiles(self.h, tn, sz, vp(hptr), vp(hlist), vp(tslot), vp(nslot), vp(lslot)) == 0
         return hptr, hlist[:nh], tslot.reshape(-1, 4), nslot, lslot[:len(self.llist) // 2], hmax
+
+    def tile_runs(self, tn):
+        """(rptr, runs (nruns, 2) as (first node, count)) of build_tiles."""
+        L = lib()
+        nr = L.probe_tile_runs(self.h, tn, None, None)
+        assert nr >= 0
+        nt = (int(self.scalars[0]) + tn - 1) // tn
+        rptr = np.zeros(nt + 1, np.int32)
+        runs = np.zeros(max(2 * nr, 2), np.int32)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        assert L.probe_tile_runs(self.h, tn, vp(rptr), vp(runs)) == nr
+        return rptr, runs[:2 * nr].reshape(-1, 2)
+
+    def pipe_pack(self, tn, max_runs=64):
+        """(hdr (ntiles, 4), runs (ntiles, max_runs, 2), nrec (n_active, 8),
+        tpack, tmax) of build_pipe_pack, or None when the model does not fit."""
+        L = lib()
+        sz = (C.c_int * 5)()
+        rc = L.probe_pipe_pack(self.h, tn, max_runs, sz, None, None, None, None)
+        if rc == 1:
+            return None
+        assert rc == 0
+        arrs = [np.zeros(max(sz[i], 1), np.int32) for i in range(4)]
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        assert L.probe_pipe_pack(self.h, tn, max_runs, sz, *[vp(a) for a in arrs]) == 0
+        hdr, runs, nrec, tpack = [a[:sz[i]] for i, a in enumerate(arrs)]
+        return hdr.reshape(-1, 4), runs.reshape(-1, max_runs, 2), nrec.reshape(-1, 8), tpack, sz[4]
 
     def wave(self, r, t, x1, x3):
         out = np.zeros(6)

@@ -37,6 +37,11 @@ def test_closed_form_q4_matches_calck():
                 a, b = np.zeros(1), np.zeros(1)
                 L.probe_q4_ku_corner(*k, npb.dp(ux), npb.dp(uy), c, npb.dp(a), npb.dp(b))
                 assert abs(a[0] - fx[c]) <= 1e-14 * np.abs(f).max() and abs(b[0] - fy[c]) <= 1e-14 * np.abs(f).max()
+                # the folded form of the FP32 kernels: -w times the corner force
+                for w in (1.0, 0.5):
+                    L.probe_q4_corner_acc(*k, npb.dp(ux), npb.dp(uy), c, w, npb.dp(a), npb.dp(b))
+                    tol = 1e-14 * np.abs(f).max()
+                    assert abs(a[0] + w * fx[c]) <= tol and abs(b[0] + w * fy[c]) <= tol
 
 
 @pytest.mark.parametrize("kind", [1, 2, 4, 5, 6])
@@ -130,6 +135,98 @@ def test_tile_halo_slots_point_at_the_right_nodes(tn):
     link_node = np.repeat(np.arange(na), np.diff(P.lptr))
     if link_node.size:
         assert np.array_equal(hlist[hptr[node_tile[link_node]] + lslot], P.llist.reshape(-1, 2)[:, 1])
+
+
+def _u16(a):
+    return np.asarray(a, np.int64) & 0xFFFF
+
+
+@pytest.mark.parametrize("name,tn", [("canyon", 8), ("canyon", 16), ("valley", 16), ("valley", 32)])
+def test_pipeline_copies_cover_the_halo_and_stay_in_their_stage(name, tn):
+    """The copies k_pipe32's producer warp issues per tile, replayed on the
+    host with its own arithmetic (lane i takes runs i and 32 + i, slots by a
+    scan of the run lengths): the halo runs rebuild the sorted halo exactly,
+    every copy lands inside its region of the stage, every address and size
+    is a multiple of 16 bytes, and the byte total is the expect_tx count."""
+    m = workloads.build(name, scale=0.1, steps=5)
+    P = npb.PlanView(m)
+    na, nn = int(P.scalars[0]), m.nnodes
+    hptr, hlist, tslot, nslot, lslot, hmax = P.tiles(tn)
+    hdr, runs, nrec, tpack, tmax = P.pipe_pack(tn)
+    assert len(hdr) == len(hptr) - 1
+    for R in (4, 64):
+        tmev = (tmax + 1) & ~1
+        off = [hmax * 8 * R]
+        off += [off[0] + tn * 8 * R, off[0] + tn * 12 * R, off[0] + tn * 16 * R, off[0] + tn * 16 * R + tn * 32]
+        off.append(off[4] + (tmev * 8 + 15) // 16 * 16)
+        stage = (off[5] + tmax * 16 + 127) // 128 * 128
+        region_end = [off[0], off[1], off[2], off[3], off[4], off[5], stage]
+        for t in range(len(hdr)):
+            hc, nt, toff, nr = hdr[t]
+            assert hc == hptr[t + 1] - hptr[t] and nr <= 64
+            r = runs[t]
+            assert (r[nr:, 1] == 0).all() and (r[:nr, 1] > 0).all() and (r[:nr].sum(axis=1) <= nn).all()
+            nodes = np.concatenate([np.arange(a, a + c) for a, c in r[:nr]])
+            assert np.array_equal(nodes, hlist[hptr[t]:hptr[t + 1]])
+            ca, cb = r[:32, 1], r[32:, 1]
+            offa = np.cumsum(ca) - ca
+            offb = ca.sum() + np.cumsum(cb) - cb
+            cnt = min(tn, na - t * tn)
+            ntev = (nt + 1) & ~1
+            copies = []   # (region, dst offset, src byte offset in its array, bytes)
+            for lane in range(32):
+                for (first, c), o in ((r[lane], offa[lane]), (r[32 + lane], offb[lane])):
+                    if c:
+                        copies.append((0, o * 8 * R, first * 8 * R, c * 8 * R))
+            n0 = t * tn
+            copies += [(1, off[0], n0 * 8 * R, cnt * 8 * R), (2, off[1], n0 * 4 * R, cnt * 4 * R),
+                       (3, off[2], n0 * 4 * R, cnt * 4 * R), (4, off[3], n0 * 32, cnt * 32)]
+            if nt:
+                copies += [(5, off[4], toff * 16, ntev * 8), (6, off[5], toff * 16 + ntev * 8, nt * 16)]
+            total = 0
+            for reg, dst, src, nb in copies:
+                lo = 0 if reg == 0 else region_end[reg - 1]
+                assert dst % 16 == 0 and src % 16 == 0 and nb % 16 == 0 and nb > 0
+                assert lo <= dst and dst + nb <= region_end[reg]
+                total += nb
+            assert total == hc * 8 * R + cnt * (16 * R + 32) + ntev * 8 + nt * 16 < 2 ** 20
+            assert toff * 4 + 2 * ntev + 4 * nt <= len(tpack)
+
+
+@pytest.mark.parametrize("name,tn", [("canyon", 8), ("valley", 16)])
+def test_pipeline_records_decode_to_the_mesh(name, tn):
+    """The node and term records, decoded as k_pipe32's consumers decode
+    them, give back each node's terms in gather order: corners through the
+    halo slots, the corner the node occupies, the element coefficients times
+    the term weight, the node's own slot, DRM and anchor-link ranges."""
+    m = workloads.build(name, scale=0.1, steps=5)
+    P = npb.PlanView(m)
+    na = int(P.scalars[0])
+    hptr, hlist, tslot, nslot, lslot, hmax = P.tiles(tn)
+    hdr, runs, nrec, tpack, tmax = P.pipe_pack(tn)
+    econn = P.econn.reshape(-1, 4)
+    ecoef = np.asarray(P.ecoef, np.float64).reshape(-1, 4).astype(np.float32)
+    tp = tpack.view(np.uint32)
+    for n in range(na):
+        t = n // tn
+        hc, nt, toff, nr = hdr[t]
+        ntev = (nt + 1) & ~1
+        meta = nrec[n, 4:].view(np.uint32)
+        tb, tc = int(meta[0] & 0xFFFF), int(meta[0] >> 16)
+        assert tc == P.tptr[n + 1] - P.tptr[n] and tb == P.tptr[n] - P.tptr[t * tn]
+        assert hlist[hptr[t] + int(meta[1])] == n
+        assert int(meta[2] & 0xFFFFFF) == P.dptr[n] and int(meta[2] >> 24) == P.dptr[n + 1] - P.dptr[n]
+        assert int(meta[3] & 0xFFFFFF) == P.lptr[n] and int(meta[3] >> 24) == P.lptr[n + 1] - P.lptr[n]
+        for j in range(tc):
+            q = P.tptr[n] + j
+            ent = int(P.tlist[q])
+            e, cor, w = (ent >> 1) >> 2, (ent >> 1) & 3, 0.5 if ent & 1 else 1.0
+            x, y = tp[4 * toff + 2 * (tb + j)], tp[4 * toff + 2 * (tb + j) + 1]
+            slots = [x & 0x3FFF, x >> 16, y & 0xFFFF, y >> 16]
+            assert (x >> 14) & 3 == cor
+            assert np.array_equal(hlist[hptr[t] + np.array(slots, np.int64)], econn[e])
+            k = tpack[4 * toff + 2 * ntev + 4 * (tb + j):][:4].view(np.float32)
+            assert np.array_equal(k, ecoef[e] * np.float32(w))
 
 
 @pytest.mark.parametrize("name,scale,steps,kw", [("homogeneous_rectangle", 0.125, 250, {}),

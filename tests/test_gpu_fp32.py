@@ -47,7 +47,7 @@ def test_canyon_fp32_every_rhs_vs_oracle(variant):
         assert per_receiver_rel(g[r], o["seis"]).max() <= TOL, r
 
 
-@pytest.mark.parametrize("variant,rpt", [(0, 1), (0, 2), (0, 4), (1, 1), (1, 2), (1, 4)])
+@pytest.mark.parametrize("variant,rpt", [(0, 1), (0, 2), (0, 4), (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4)])
 def test_batched_valley_rhs_match_oracle_for_every_kernel_and_tile(variant, rpt):
     m = workloads.build("valley_batched", scale=0.1, steps=500, save_every=5)
     assert m.problem.nrhs == 64
@@ -107,12 +107,52 @@ def test_autotuner_picks_a_working_shape():
     m = workloads.build("valley_batched", scale=0.1, steps=40)
     choice = autotune.tune(m, steps=8, warmup=2)
     assert choice["rhs_per_thread"] in (1, 2, 4) and choice["block_threads"] in (128, 256, 512)
-    assert choice["variant"] in (0, 1) and len(choice["tried"]) >= 12
+    assert choice["variant"] in (0, 1, 2) and len(choice["tried"]) >= 18
 
 
 def test_tiled_and_direct_kernels_agree():
+    """The tiled kernel sums the same terms in the same order as the direct
+    gather, from shared memory: bit for bit the same state."""
     m = workloads.build("canyon", scale=0.2, steps=300, save_every=3)
-    a, _ = run32(m, variant=0)
-    b, _ = run32(m, variant=1)
+    a, ua = run32(m, variant=0)
+    b, ub = run32(m, variant=1)
+    assert np.array_equal(a, b)
     for r in range(m.problem.nrhs):
-        assert per_receiver_rel(a[r], b[r]).max() <= 1e-6
+        assert np.array_equal(ua[r], ub[r]), r
+
+
+EIGHT_WAVES = [("WAVEP", 0.0), ("WAVEP", 20.0), ("WAVEP", 40.0), ("WAVEP", 60.0),
+               ("WAVESV", 0.0), ("WAVESV", 10.0), ("WAVESV", 20.0), ("WAVESV", 25.0)]
+
+
+@pytest.mark.parametrize("block,rpt", [(256, 4), (128, 2), (512, 4)])
+def test_pipelined_kernel_runs_and_matches_the_direct_gather(block, rpt):
+    """Variant 2 (bulk-copy pipeline) on a refined canyon with 8 waves:
+    k_pipe32 is what runs; it sums the same terms in the same order as the
+    direct gather (weights folded into the coefficients by a power of two),
+    so seismograms and final state are bit for bit the same; and both match
+    the oracle."""
+    m = workloads.build("canyon", scale=0.2, steps=300, save_every=3, waves=EIGHT_WAVES)
+    assert m.problem.nhanging > 0 and m.problem.nrhs == 8
+    with Solver(m, precision=EXFEM_FP32_KAHAN, variant=2, block_threads=block, rhs_per_thread=rpt) as s:
+        s.init_explicit()
+        names = s.kernel_times(4)
+        assert "k_pipe32" in names and "k_step32" not in names, names
+    a, ua = run32(m, variant=0)
+    b, ub = run32(m, variant=2, block_threads=block, rhs_per_thread=rpt)
+    assert np.array_equal(a, b)
+    for r in range(m.problem.nrhs):
+        assert np.array_equal(ua[r], ub[r]), r
+    for r in (0, 5):
+        o = oracle.run(m, rhs=r, nthreads=NT)
+        assert per_receiver_rel(b[r], o["seis"]).max() <= TOL, r
+
+
+def test_pipelined_variant_falls_back_when_rows_are_not_16_bytes():
+    """6 right-hand sides give 24-byte rows: variant 2 runs the direct gather."""
+    m = workloads.build("canyon", scale=0.15, steps=40, save_every=2)
+    assert m.problem.nrhs % 4 != 0
+    with Solver(m, precision=EXFEM_FP32_KAHAN, variant=2) as s:
+        s.init_explicit()
+        names = s.kernel_times(4)
+    assert "k_step32" in names and "k_pipe32" not in names
