@@ -55,6 +55,11 @@ struct DevModel {
     const float *hcoef4;           // per hanging entry: -2 a2 C (x, y), a1 M + a2 C (x, y)
     float *fdrm32;                 // ns * 8 * R DRM forces (FP64 math, stored FP32)
     const int *tcorn;              // 4 per gather term: the corners of its element
+    // point source (EXFEM_POINT_*; 0 = none)
+    int point_kind, npoint;
+    double point_amp, point_sigma, point_t0;
+    const unsigned char *pflag;    // per internal node: 1 on a source node (or null)
+    const int *pnodes;             // the source nodes (internal ids)
     // mutable state
     double *fdrm;            // ns * 16 * R DRM forces (stiffness part, mass part)
     double *seis;            // R * nsave * nrecv * 2
@@ -87,6 +92,11 @@ struct Ctx {
     size_t tile_smem = 0;
     const int *t_hptr = nullptr, *t_hlist = nullptr, *t_nslot = nullptr, *t_lslot = nullptr;
     const unsigned short *t_tslot = nullptr;
+    // point source in the FP32 form: the active nodes it acts on and their
+    // weights (1 on a source node, 1/2 per hanging source node anchored)
+    const int *p32_node = nullptr;
+    const float *p32_w = nullptr;
+    int p32_n = 0;
     // bulk-copy pipeline of the FP32 step (variant 2): per-tile headers and
     // halo runs, node records, term records; persistent grid
     bool use_pipe = false;

@@ -95,6 +95,19 @@ __host__ __device__ __forceinline__ void q4_msq(const T v[4], T out[4]) {
         out[k] = (T(4) * v[k] + T(2) * v[(k + 1) & 3] + v[(k + 2) & 3] + T(2) * v[(k + 3) & 3]) / T(9);
 }
 
+// The point-source pulse, ricker (formulation.f90:53-59), in its operation
+// order: amp * exp(-t^2/(4 sigma)) (t^2 - 2 sigma) / (8 sqrt(pi) sigma^2.5).
+__host__ __device__ __forceinline__ double point_ricker(double amp, double sigma, double t) {
+    double r = exp(-(t * t) / (4.0 * sigma)) * (t * t - 2.0 * sigma) /
+               (8.0 * sqrt(3.14159265358979323846) * pow(sigma, 2.5));
+    return r * amp;
+}
+
+// The source's value at step `step` (time step * dt).
+__device__ __forceinline__ double point_value(const DevModel &m, int step) {
+    return point_ricker(m.point_amp, m.point_sigma, (double)step * m.dt - m.point_t0);
+}
+
 // One Ricker term with its first two time derivatives (pwaves.f90:157-169).
 __host__ __device__ __forceinline__ void ricker3(double fp, double d, double out[3]) {
     double q = fp * d;

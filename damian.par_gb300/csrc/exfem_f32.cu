@@ -12,8 +12,9 @@
 // 12 bytes per dof: u_hi 4 + u_comp 2 + D 4 + D_comp 2.
 // Anchors of hanging nodes add half of each hanging node's term
 // (sum_reactanchors, halving form); in the increment form that carries
-// D_h ((u_b - u_a)/2 + (D_h - D_a)) because the hanging node's mass acts on
-// its own displacement and increment.  Templates, masses, dashpots, hanging
+// D_h ((u_h - u_a) + (D_h - D_a)) because the hanging node's mass acts on
+// its own displacement and increment (read from its row, which holds the
+// anchor average after every step and a prescribed displacement at t = 0).  Templates, masses, dashpots, hanging
 // weights and dt stay FP64 on the host and are rounded once.
 //
 // One step is three kernels:
@@ -262,23 +263,22 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     Vec<RPT>::load(uh + bn, unx);
     Vec<RPT>::load(uh + bn + R, uny);
     // hanging nodes this node anchors:
-    //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_b - u_n)/2 + (D_h - D_n)) ]
-    // (D_b - D_n = 2 (D_h - D_n); D_h is read instead of D_b because the
-    // other anchor's thread rewrites D_b in place during this kernel, while
-    // D_h changes only in k_hang32)
+    //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_h - u_n) + (D_h - D_n)) ]
+    // (u_h, D_h from the hanging node's rows, which change only in k_hang32;
+    // the other anchor's row is rewritten in place during this kernel)
     for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
-        int h = __ldg(m.llist + 2 * q), b = __ldg(m.llist + 2 * q + 1);
+        int h = __ldg(m.llist + 2 * q);
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
-        size_t bh = ((size_t)h * 2) * R + r0, bb = ((size_t)b * 2) * R + r0;
-        float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
+        size_t bh = ((size_t)h * 2) * R + r0;
+        float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
         Vec<RPT>::load_cg(dh + bh, hx);
         Vec<RPT>::load_cg(dh + bh + R, hy);
-        Vec<RPT>::load(uh + bb, ubx);
-        Vec<RPT>::load(uh + bb + R, uby);
+        Vec<RPT>::load(uh + bh, uhx);
+        Vec<RPT>::load(uh + bh + R, uhy);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
-            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j]) + (hx[j] - dx[j])));
-            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j]) + (hy[j] - dy[j])));
+            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * ((uhx[j] - unx[j]) + (hx[j] - dx[j])));
+            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * ((uhy[j] - uny[j]) + (hy[j] - dy[j])));
         }
     }
     // delta = r / m_full; D+ = D + delta and u+ = u + D+, both Kahan-compensated
@@ -419,15 +419,15 @@ __global__ void __launch_bounds__(512) k_tile32(DevModel m, TileArgs ta, const f
         int sb = __ldg(ta.lslot + q);
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
         size_t bh = ((size_t)h * 2) * R + r0;
-        float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
+        float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
         Vec<RPT>::load_cg(dh + bh, hx);
         Vec<RPT>::load_cg(dh + bh + R, hy);
-        VecS<RPT>::load(sm + sb * row + rl, ubx);
-        VecS<RPT>::load(sm + sb * row + RC + rl, uby);
+        VecS<RPT>::load(sm + sb * row + rl, uhx);
+        VecS<RPT>::load(sm + sb * row + RC + rl, uhy);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
-            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j]) + (hx[j] - dx[j])));
-            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j]) + (hy[j] - dy[j])));
+            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * ((uhx[j] - unx[j]) + (hx[j] - dx[j])));
+            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * ((uhy[j] - uny[j]) + (hy[j] - dy[j])));
         }
     }
     float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
@@ -493,7 +493,7 @@ struct PipeArgs {
     const int2 *runs;       // per tile: PIPE_RUNS (first node, count), count 0 past the last
     const int4 *nrec;       // per active node: 2 int4 (node record)
     const int4 *tpack;      // term records, per tile
-    const int *lslot;       // per anchor link: halo slot of the other anchor
+    const int *lslot;       // per anchor link: halo slot of the hanging node
     int tn, ntiles, nstage;
     unsigned stage_bytes;   // one stage; regions at the offsets below
     unsigned off_dh, off_dc, off_uc, off_nrec, off_ts, off_tk;
@@ -714,15 +714,15 @@ __global__ void __launch_bounds__(544) k_pipe32(DevModel m, PipeArgs pa, const f
                 int sb = __ldg(pa.lslot + q);
                 float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (hn - m.n_active));
                 size_t bh = ((size_t)hn * 2) * R + r0;
-                float hx[RPT], hy[RPT], ubx[RPT], uby[RPT];
+                float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
                 Vec<RPT>::load_cg(dh + bh, hx);
                 Vec<RPT>::load_cg(dh + bh + R, hy);
-                VecS<RPT>::load(sh + sb * row + rl, ubx);
-                VecS<RPT>::load(sh + sb * row + R + rl, uby);
+                VecS<RPT>::load(sh + sb * row + rl, uhx);
+                VecS<RPT>::load(sh + sb * row + R + rl, uhy);
 #pragma unroll
                 for (int j = 0; j < RPT; ++j) {
-                    ax[j] += 0.5f * (hc.x * hx[j] + hc.z * (0.5f * (ubx[j] - unx[j]) + (hx[j] - dx[j])));
-                    ay[j] += 0.5f * (hc.y * hy[j] + hc.w * (0.5f * (uby[j] - uny[j]) + (hy[j] - dy[j])));
+                    ax[j] += 0.5f * (hc.x * hx[j] + hc.z * ((uhx[j] - unx[j]) + (hx[j] - dx[j])));
+                    ay[j] += 0.5f * (hc.y * hy[j] + hc.w * ((uhy[j] - uny[j]) + (hy[j] - dy[j])));
                 }
             }
             float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
@@ -759,15 +759,68 @@ __global__ void __launch_bounds__(544) k_pipe32(DevModel m, PipeArgs pa, const f
     }
 }
 
+// Point source in the FP32 form, after the step kernel and before k_hang32
+// (the force enters delta linearly, so the step kernels stay untouched).
+//   POINTN: the y dof of node p32_node[i] gets w_i f(t) / m_full added to D+
+//           and to u+ (point_reactions before sum_reactanchors: a hanging
+//           source node gives each anchor half its force).
+//   POINTD: u+ = f(t) on the source node's y dof, D+ = f(t) - u, with u the
+//           displacement before the step (point_displacements after the
+//           update, explicit.f90:150).
+// Values are recombined and re-split (hi - comp) in FP64.
+__global__ void k_point32(DevModel m, const int *__restrict__ pn, const float *__restrict__ pw, int np,
+                          float *__restrict__ uhn, unsigned short *__restrict__ uc, float *__restrict__ dh,
+                          unsigned short *__restrict__ dc) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)np * m.R) return;
+    const int i = (int)(t / m.R), r = (int)(t % m.R);
+    const int n = pn[i];
+    const size_t iy = ((size_t)n * 2 + 1) * m.R + r;
+    const double f = point_value(m, read_step(m) + 1);
+    const double u1 = (double)uhn[iy] - (double)bf2f(uc[iy]);
+    const double d1 = (double)dh[iy] - (double)bf2f(dc[iy]);
+    double u2, d2;
+    if (m.point_kind == EXFEM_POINT_FORCE) {
+        const double dp = (double)pw[i] * f * (double)reinterpret_cast<const float4 *>(m.ncoef4)[n].y;
+        u2 = u1 + dp;
+        d2 = d1 + dp;
+    } else {
+        u2 = f;
+        d2 = f - (u1 - d1);
+    }
+    const float uh2 = (float)u2, dh2 = (float)d2;
+    uhn[iy] = uh2;
+    uc[iy] = f2bf((float)((double)uh2 - u2));
+    dh[iy] = dh2;
+    dc[iy] = f2bf((float)((double)dh2 - d2));
+}
+
+// A prescribed displacement at t = 0 and -dt on every source node (hanging
+// ones included): u = v0, D = v0 - vm (explicit.f90:93-94).
+__global__ void k_point_init32(DevModel m, float *__restrict__ uh, unsigned short *__restrict__ uc,
+                               float *__restrict__ dh, unsigned short *__restrict__ dc, double v0, double vm) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.npoint * m.R) return;
+    const int n = m.pnodes[t / m.R], r = (int)(t % m.R);
+    const size_t iy = ((size_t)n * 2 + 1) * m.R + r;
+    const double d = v0 - vm;
+    const float uh2 = (float)v0, dh2 = (float)d;
+    uh[iy] = uh2;
+    uc[iy] = f2bf((float)((double)uh2 - v0));
+    dh[iy] = dh2;
+    dc[iy] = f2bf((float)((double)dh2 - d));
+}
+
 // u of one node in FP64 (u_hi - comp); hanging corners read as anchor averages.
+// (rows: read a hanging corner's own row, for the step-0 sample.)
 __device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, const unsigned short *uc, int node,
-                                         int r, double &vx, double &vy) {
+                                         int r, bool rows, double &vx, double &vy) {
     const size_t R = m.R;
     auto val = [&](int x, int d) {
         size_t i = ((size_t)x * 2 + d) * R + r;
         return (double)uh[i] - (double)bf2f(uc[i]);
     };
-    if (node < m.n_active) {
+    if (node < m.n_active || rows) {
         vx = val(node, 0);
         vy = val(node, 1);
     } else {
@@ -779,7 +832,7 @@ __device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, con
 }
 
 // Hanging nodes (anchor averages of u_hi, comp and D) and receivers.
-__global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ uhn,
+__global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restrict__ uho, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
                                                 unsigned short *__restrict__ dc, int nb_hang, int mode) {
     int step = (mode == 1) ? 0 : read_step(m) + 1;
@@ -789,14 +842,25 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ 
         if (mode == 0 && t < (long long)m.n_hang * m.R) {
             int i = (int)(t / m.R), r = (int)(t % m.R);
             int h = m.hang[3 * i], a = m.hang[3 * i + 1], b = m.hang[3 * i + 2];
+            // A prescribed point displacement at t = 0 (explicit.f90:93) is
+            // the one hanging value that is not its anchors' average, so at
+            // the first step the increment of such a node is new - old.
+            const bool from_row = m.point_kind == EXFEM_POINT_DISP && step == 1 && m.pflag[h];
 #pragma unroll
             for (int d = 0; d < 2; ++d) {
                 size_t ih = ((size_t)h * 2 + d) * R + r, ia = ((size_t)a * 2 + d) * R + r,
                        ib = ((size_t)b * 2 + d) * R + r;
+                const double u_old = (double)uho[ih] - (double)bf2f(uc[ih]);   // the row before this step
                 uhn[ih] = 0.5f * (uhn[ia] + uhn[ib]);
                 uc[ih] = f2bf(0.5f * (bf2f(uc[ia]) + bf2f(uc[ib])));
-                dh[ih] = 0.5f * (dh[ia] + dh[ib]);
-                dc[ih] = f2bf(0.5f * (bf2f(dc[ia]) + bf2f(dc[ib])));
+                if (from_row) {
+                    const double dn = ((double)uhn[ih] - (double)bf2f(uc[ih])) - u_old;
+                    dh[ih] = (float)dn;
+                    dc[ih] = f2bf((float)((double)dh[ih] - dn));
+                } else {
+                    dh[ih] = 0.5f * (dh[ia] + dh[ib]);
+                    dc[ih] = f2bf(0.5f * (bf2f(dc[ia]) + bf2f(dc[ib])));
+                }
             }
         }
     } else if (step % m.io == 0) {
@@ -807,7 +871,7 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, float *__restrict__ 
             double fx = 0.0, fy = 0.0;
             for (int k = 0; k < 4; ++k) {
                 double vx, vy;
-                load_u32(m, uhn, uc, m.rnode[4 * i + k], r, vx, vy);
+                load_u32(m, uhn, uc, m.rnode[4 * i + k], r, mode == 1, vx, vy);
                 double w = m.rw[4 * i + k];
                 fx += w * vx;
                 fy += w * vy;
@@ -977,6 +1041,26 @@ int f32_alloc(Ctx &c) {
     if ((rc = alloc32(c, nst, &c.ucomp))) return rc;
     if ((rc = alloc32(c, nst, &c.udel[0]))) return rc;
     if ((rc = alloc32(c, nst, &c.dcomp))) return rc;
+    // point source: the active nodes it acts on, with their weights
+    c.p32_n = 0;
+    if (P.point_kind != 0) {
+        std::vector<float> w(P.n_active, 0.f);
+        for (int n = 0; n < P.n_active; ++n) {
+            if (P.pflag[n]) w[n] += 1.f;
+            if (P.point_kind == EXFEM_POINT_FORCE)
+                for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q)
+                    if (P.pflag[P.llist[2 * (size_t)q]]) w[n] += 0.5f;
+        }
+        std::vector<int> pn;
+        std::vector<float> pw;
+        for (int n = 0; n < P.n_active; ++n)
+            if (w[n] != 0.f) { pn.push_back(n); pw.push_back(w[n]); }
+        if (!pn.empty()) {
+            if ((rc = upload32(c, pn, &c.p32_node))) return rc;
+            if ((rc = upload32(c, pw, &c.p32_w))) return rc;
+            c.p32_n = (int)pn.size();
+        }
+    }
     c.rhs_per_thread = pick_rpt(c);
     if (c.opts.block_threads <= 0) c.block_threads = 256;
     // shared-memory tiles (variant 1; variant 0, the default, is the direct gather)
@@ -1039,6 +1123,15 @@ int f32_init(Ctx &c) {
     CK(cudaMemsetAsync(c.ucomp, 0, nst * sizeof(unsigned short), c.stream));
     CK(cudaMemsetAsync(c.udel[0], 0, nst * sizeof(float), c.stream));
     CK(cudaMemsetAsync(c.dcomp, 0, nst * sizeof(unsigned short), c.stream));
+    const DevModel &m = c.dm;
+    if (m.point_kind == EXFEM_POINT_DISP && m.npoint > 0) {
+        const double v0 = point_ricker(m.point_amp, m.point_sigma, 0.0 - m.point_t0);
+        const double vm = point_ricker(m.point_amp, m.point_sigma, -m.dt - m.point_t0);
+        k_point_init32<<<nblocks((long long)m.npoint * m.R, 128), 128, 0, c.stream>>>(m, c.uhi[0], c.ucomp, c.udel[0],
+                                                                                      c.dcomp, v0, vm);
+        c.launches++;
+        CK(cudaGetLastError());
+    }
     return EXFEM_OK;
 }
 
@@ -1087,10 +1180,16 @@ int f32_launch_step(Ctx &c, int par) {
     c.launches++;
     mark(c, "k_step32");
     }
+    if (c.p32_n > 0) {
+        k_point32<<<nblocks((long long)c.p32_n * m.R, 128), 128, 0, c.stream>>>(m, c.p32_node, c.p32_w, c.p32_n, uhn,
+                                                                               c.ucomp, c.udel[0], c.dcomp);
+        c.launches++;
+        mark(c, "k_point32");
+    }
     const int TH = 256;
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + TH - 1) / TH);
     int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
-    k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0);
+    k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0);
     c.launches++;
     mark(c, "k_hang32");
     CK(cudaGetLastError());
@@ -1102,7 +1201,7 @@ int f32_launch_sample0(Ctx &c, int par) {
     const int TH = 256;
     int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
     if (nbr > 0) {
-        k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.ucomp, c.udel[0], c.dcomp, 0, 1);
+        k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.uhi[par], c.ucomp, c.udel[0], c.dcomp, 0, 1);
         c.launches++;
     }
     CK(cudaGetLastError());

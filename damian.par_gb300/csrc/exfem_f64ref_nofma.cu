@@ -142,9 +142,11 @@ __global__ void __launch_bounds__(128) k_elem_ref(DevModel m, const double *__re
     }
 }
 
-// Sum of one node's own terms in the reference order.
-__device__ __forceinline__ void own_sum(const DevModel &m, int n, int r, const double *__restrict__ ef, double &rx,
-                                        double &ry) {
+// Sum of one node's own terms in the reference order: DRM (additive_reactions,
+// explicit.f90:128), elements (129-142), then a point force on its y dof
+// (absolute_reactions, 144) at step `step`.
+__device__ __forceinline__ void own_sum(const DevModel &m, int n, int r, const double *__restrict__ ef, int step,
+                                        double &rx, double &ry) {
     const size_t R = m.R;
     rx = 0.0;
     ry = 0.0;
@@ -162,28 +164,37 @@ __device__ __forceinline__ void own_sum(const DevModel &m, int n, int r, const d
         rx = rx + ef[b];
         ry = ry + ef[b + R];
     }
+    if (m.point_kind == EXFEM_POINT_FORCE && m.pflag[n]) ry = ry + point_value(m, step);
 }
 
 __global__ void __launch_bounds__(128) k_node_ref(DevModel m, const double *__restrict__ ef, double *__restrict__ unew) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m.n_active * m.R) return;
     int n = (int)(t / m.R), r = (int)(t % m.R);
+    const int step = *(volatile int *)m.d_step + 1;
     double rx, ry;
-    own_sum(m, n, r, ef, rx, ry);
+    own_sum(m, n, r, ef, step, rx, ry);
     for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
         double hx, hy;
-        own_sum(m, m.llist[2 * q], r, ef, hx, hy);
+        own_sum(m, m.llist[2 * q], r, ef, step, hx, hy);
         rx = rx + hx / 2.0;
         ry = ry + hy / 2.0;
     }
     const size_t R = m.R;
     unew[((size_t)n * 2) * R + r] = rx / m.mfull[2 * n];
-    unew[((size_t)n * 2 + 1) * R + r] = ry / m.mfull[2 * n + 1];
+    double uy = ry / m.mfull[2 * n + 1];
+    if (m.point_kind == EXFEM_POINT_DISP && m.pflag[n]) uy = point_value(m, step);   // explicit.f90:150
+    unew[((size_t)n * 2 + 1) * R + r] = uy;
 }
 
-__device__ __forceinline__ void load_u64(const DevModel &m, const double *u, int node, int r, double &vx, double &vy) {
+// u at a receiver corner.  A hanging corner is read as set_dispshanging's
+// (u_a + u_b)/2, because the blocks writing hanging nodes run beside the
+// receiver blocks; `rows` reads its own row instead (the step-0 sample, where
+// a prescribed point displacement may differ from the average).
+__device__ __forceinline__ void load_u64(const DevModel &m, const double *u, int node, int r, bool rows, double &vx,
+                                         double &vy) {
     const size_t R = m.R;
-    if (node < m.n_active) {
+    if (node < m.n_active || rows) {
         vx = u[((size_t)node * 2) * R + r];
         vy = u[((size_t)node * 2 + 1) * R + r];
     } else {   // hanging corner: set_dispshanging value (u_a + u_b)/2
@@ -216,7 +227,7 @@ __global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict
             double fx = 0.0, fy = 0.0;
             for (int k = 0; k < 4; ++k) {
                 double vx, vy;
-                load_u64(m, unew, m.rnode[4 * i + k], r, vx, vy);
+                load_u64(m, unew, m.rnode[4 * i + k], r, mode == 1, vx, vy);
                 double w = m.rw[4 * i + k];
                 fx = fx + w * vx;
                 fy = fy + w * vy;

@@ -128,6 +128,17 @@ __global__ void __launch_bounds__(256) k_elem64(DevModel m, const double *__rest
 }
 
 // --------------------------------------------------------------- nodes ----
+// Point force on the y dof (absolute_reactions, explicit.f90:144): the node's
+// own, and half of each hanging source node it anchors (sum_reactanchors).
+__device__ __forceinline__ void point_terms(const DevModel &m, int n, double &rx, double &ry) {
+    (void)rx;
+    if (m.point_kind != EXFEM_POINT_FORCE) return;
+    const int step = read_step(m) + 1;
+    if (m.pflag[n]) ry += point_value(m, step);
+    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q)
+        if (m.pflag[m.llist[2 * q]]) ry += 0.5 * point_value(m, step);
+}
+
 __global__ void __launch_bounds__(256) k_node64(DevModel m, const double *__restrict__ ef,
                                                 double *__restrict__ unew) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -152,8 +163,11 @@ __global__ void __launch_bounds__(256) k_node64(DevModel m, const double *__rest
             rx += w * v.x;
             ry += w * v.y;
         }
+        point_terms(m, n, rx, ry);
         double2 im = reinterpret_cast<const double2 *>(m.inv_mfull)[n];
-        reinterpret_cast<double2 *>(unew)[n] = make_double2(rx * im.x, ry * im.y);
+        double uy = ry * im.y;
+        if (m.point_kind == EXFEM_POINT_DISP && m.pflag[n]) uy = point_value(m, read_step(m) + 1);
+        reinterpret_cast<double2 *>(unew)[n] = make_double2(rx * im.x, uy);
     } else {
         for (int q = q0; q < q1; ++q) {
             int ent = __ldg(m.tlist + q);
@@ -163,12 +177,23 @@ __global__ void __launch_bounds__(256) k_node64(DevModel m, const double *__rest
             rx += w * ef[base];
             ry += w * ef[base + m.R];
         }
+        point_terms(m, n, rx, ry);
+        double uy = ry * m.inv_mfull[2 * n + 1];
+        if (m.point_kind == EXFEM_POINT_DISP && m.pflag[n]) uy = point_value(m, read_step(m) + 1);
         unew[((size_t)n * 2) * m.R + r] = rx * m.inv_mfull[2 * n];
-        unew[((size_t)n * 2 + 1) * m.R + r] = ry * m.inv_mfull[2 * n + 1];
+        unew[((size_t)n * 2 + 1) * m.R + r] = uy;
     }
 }
 
 inline int nblocks(long long work, int threads) { return (int)std::max<long long>(1, (work + threads - 1) / threads); }
+
+// A prescribed point displacement v on the y dof of every source node.
+__global__ void k_point_set64(DevModel m, double *u, double v) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.npoint * m.R) return;
+    const int n = m.pnodes[t / m.R], r = (int)(t % m.R);
+    u[((size_t)n * 2 + 1) * m.R + r] = v;
+}
 
 int launch_step64(Ctx &c, int par) {
     DevModel &m = c.dm;
@@ -272,6 +297,21 @@ int setup_device(Ctx &c) {
         d.inv_beta = 1.0 / w.beta;
     }
     TRY(upload(c, dw, &m.waves));
+    m.point_kind = P.point_kind;
+    m.point_amp = P.point_amp;
+    m.point_sigma = P.point_sigma;
+    m.point_t0 = P.point_t0;
+    m.pflag = nullptr;
+    m.pnodes = nullptr;
+    m.npoint = 0;
+    if (P.point_kind != 0) {
+        std::vector<int> pn;
+        for (int n = 0; n < P.nn; ++n)
+            if (P.pflag[n]) pn.push_back(n);
+        TRY(upload(c, P.pflag, &m.pflag));
+        m.npoint = (int)pn.size();
+        if (!pn.empty()) TRY(upload(c, pn, &m.pnodes));
+    }
     TRY(dalloc(c, (size_t)std::max(m.ns, 1) * 16 * P.R, &m.fdrm));
     TRY(dalloc(c, (size_t)P.R * P.nsave * std::max(P.nrecv, 1) * 2, &m.seis));
     int *ctr = nullptr;
@@ -432,6 +472,14 @@ int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out) {
         size_t nst = (size_t)c.plan.nn * 2 * c.plan.R;
         CK(cudaMemsetAsync(c.u64[0], 0, nst * sizeof(double), c.stream));
         CK(cudaMemsetAsync(c.u64[1], 0, nst * sizeof(double), c.stream));
+        if (m.point_kind == EXFEM_POINT_DISP && m.npoint > 0) {   // explicit.f90:93-94
+            const int nb = nblocks((long long)m.npoint * m.R, 128);
+            k_point_set64<<<nb, 128, 0, c.stream>>>(m, c.u64[0], point_ricker(m.point_amp, m.point_sigma, 0.0 - m.point_t0));
+            k_point_set64<<<nb, 128, 0, c.stream>>>(m, c.u64[1],
+                                                    point_ricker(m.point_amp, m.point_sigma, -m.dt - m.point_t0));
+            c.launches += 2;
+            CK(cudaGetLastError());
+        }
     } else {
         int rc = f32_init(c);
         if (rc) return rc;
@@ -656,6 +704,7 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
         b += 8 * (nn + 2) + 12 * H + 8 * (4 * ne + 4 * nh) + 4 * nn + 4 * nh;
     }
     if (!f64) b += 16 * (4 * ne + 4 * nh);   // per-term corners of the direct gather
+    if (prob->point_kind) b += nn + 4 * (size_t)std::max(prob->npoint, 0) + 1024;   // source flags and nodes
     return b + 64 * 1024;
 }
 

@@ -125,8 +125,18 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         err = "mesh arrays missing or empty";
         return EXFEM_E_ARG;
     }
-    if (prob.nmat <= 0 || !prob.matconst || !prob.absorbing || prob.nrhs <= 0 || !prob.waves) {
-        err = "problem arrays missing (matconst/absorbing/waves)";
+    if (prob.nmat <= 0 || !prob.matconst || !prob.absorbing || prob.nrhs <= 0 || (!prob.waves && prob.nseismic > 0)) {
+        err = "problem arrays missing (matconst/absorbing, or waves with a DRM layer)";
+        return EXFEM_E_ARG;
+    }
+    if (prob.point_kind != 0 && prob.point_kind != EXFEM_POINT_FORCE && prob.point_kind != EXFEM_POINT_DISP) {
+        err = "unknown point source kind";
+        return EXFEM_E_ARG;
+    }
+    if (prob.point_kind != 0 &&
+        (prob.npoint < 0 || (prob.npoint > 0 && !prob.point_nodes) || !(prob.point_sigma > 0) ||
+         !std::isfinite(prob.point_amp) || !std::isfinite(prob.point_t0))) {
+        err = "point source needs npoint >= 0 node ids, sigma > 0 and finite amplitude and start";
         return EXFEM_E_ARG;
     }
     if (!(prob.deltat > 0) || prob.nsteps < 0 || prob.io_interval < 1) {
@@ -428,11 +438,33 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         P.rxy[2 * i] = px;
         P.rxy[2 * i + 1] = py;
     }
-    // ---- waves
+    // ---- waves (none: zero amplitudes, and no receiver adds a free field)
     P.waves.resize(P.R);
+    P.have_waves = prob.waves != nullptr;
     for (int r = 0; r < P.R; ++r) {
+        if (!prob.waves) {
+            P.waves[r] = WaveConst();
+            P.waves[r].kind = EXFEM_WAVE_P;
+            P.waves[r].alpha = P.waves[r].beta = 1.0;
+            P.waves[r].cose = 1.0;
+            continue;
+        }
         int rc = init_wave_const(prob.waves[r], prob.walpha, prob.wbeta, P.waves[r], err);
         if (rc) { err = "rhs " + std::to_string(r) + ": " + err; return rc; }
+    }
+    if (!prob.waves) P.rsoil.assign(P.nrecv, 0);
+    // ---- point source: flags on internal nodes
+    P.point_kind = prob.point_kind;
+    P.point_amp = prob.point_amp;
+    P.point_sigma = prob.point_sigma;
+    P.point_t0 = prob.point_t0;
+    P.pflag.assign(P.nn, 0);
+    if (prob.point_kind != 0) {
+        for (int i = 0; i < prob.npoint; ++i) {
+            const int g = prob.point_nodes[i];
+            if (g < 1 || g > nn) { err = "point source node out of range"; return EXFEM_E_ARG; }
+            P.pflag[P.node_of_ref[g - 1]] = 1;
+        }
     }
     return EXFEM_OK;
 }
@@ -457,7 +489,7 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
                 int e = (P.tlist[q] >> 1) >> 2;
                 for (int v = 0; v < 4; ++v) nodes.push_back(P.econn[(size_t)e * 4 + v]);
             }
-            for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) nodes.push_back(P.llist[2 * (size_t)q + 1]);
+            for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) nodes.push_back(P.llist[2 * (size_t)q]);
         }
         std::sort(nodes.begin(), nodes.end());
         nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
@@ -480,7 +512,7 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
                 int e = (P.tlist[q] >> 1) >> 2;
                 for (int v = 0; v < 4; ++v) T.tslot[4 * (size_t)q + v] = (unsigned short)slot[P.econn[(size_t)e * 4 + v]];
             }
-            for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) T.lslot[q] = slot[P.llist[2 * (size_t)q + 1]];
+            for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) T.lslot[q] = slot[P.llist[2 * (size_t)q]];
         }
         for (int x : nodes) slot[x] = -1;
     }

@@ -66,8 +66,13 @@ struct Plan {
     std::vector<int> rsoil;
     std::vector<double> rxy;
     int nrecv = 0;
-    // waves
+    // waves (have_waves false: zero-amplitude placeholders, no free field)
     std::vector<WaveConst> waves;
+    bool have_waves = true;
+    // point source (EXFEM_POINT_*): per internal node, 1 on the source nodes
+    int point_kind = 0;
+    double point_amp = 0, point_sigma = 1, point_t0 = 0;
+    std::vector<unsigned char> pflag;
     double worigin[2] = {0, 0};
     // per active node: hanging links (h, other anchor) in m_hanging order
     std::vector<int> lptr, llist;   // llist entries: h internal, b internal (pairs)
@@ -87,7 +92,7 @@ struct Tiles {
     std::vector<int> hptr, hlist;      // halo node ids per tile (sorted)
     std::vector<unsigned short> tslot; // 4 per gather term: halo slots of the element's corners
     std::vector<int> nslot;            // per active node: its own halo slot
-    std::vector<int> lslot;            // per anchor link: halo slot of the other anchor
+    std::vector<int> lslot;            // per anchor link: halo slot of the hanging node
     // runs of consecutive node ids in each tile's sorted halo (for bulk copies)
     std::vector<int> rptr;             // ntiles + 1
     std::vector<int> runs;             // (first node, count) pairs

@@ -28,7 +28,7 @@ struct Req {
     int status = EXFEM_OK;
     std::string err;
     // deep copies of the caller's arrays and the views over them
-    std::vector<int> eptr, eind, ematprop, absorbing, hanging, seismic, recv_elem;
+    std::vector<int> eptr, eind, ematprop, absorbing, hanging, seismic, recv_elem, point_nodes;
     std::vector<unsigned char> ediv;
     std::vector<double> nodes, matconst, recv_xy;
     std::vector<exfem_wave> waves;
@@ -276,7 +276,8 @@ int exfem_srv_submit(exfem_srv *s, const exfem_mesh *mesh, const exfem_problem *
         copy_arr(r->absorbing, prob->absorbing, (size_t)mesh->nnodes);
         if (prob->nhanging) copy_arr(r->hanging, prob->hanging, 3 * (size_t)prob->nhanging);
         if (prob->nseismic) copy_arr(r->seismic, prob->seismic, 2 * (size_t)prob->nseismic);
-        copy_arr(r->waves, prob->waves, (size_t)prob->nrhs);
+        if (prob->waves) copy_arr(r->waves, prob->waves, (size_t)prob->nrhs);
+        if (prob->npoint > 0 && prob->point_nodes) copy_arr(r->point_nodes, prob->point_nodes, (size_t)prob->npoint);
         if (prob->nrecv) {
             copy_arr(r->recv_xy, prob->recv_xy, 2 * (size_t)prob->nrecv);
             copy_arr(r->recv_elem, prob->recv_elem, (size_t)prob->nrecv);
@@ -292,7 +293,8 @@ int exfem_srv_submit(exfem_srv *s, const exfem_mesh *mesh, const exfem_problem *
     r->prob.matconst = r->matconst.data(); r->prob.absorbing = r->absorbing.data();
     r->prob.hanging = r->hanging.empty() ? nullptr : r->hanging.data();
     r->prob.seismic = r->seismic.empty() ? nullptr : r->seismic.data();
-    r->prob.waves = r->waves.data();
+    r->prob.waves = r->waves.empty() ? nullptr : r->waves.data();
+    r->prob.point_nodes = r->point_nodes.empty() ? nullptr : r->point_nodes.data();
     r->prob.recv_xy = r->recv_xy.empty() ? nullptr : r->recv_xy.data();
     r->prob.recv_elem = r->recv_elem.empty() ? nullptr : r->recv_elem.data();
     r->prob.nsteps = nsteps;

@@ -22,6 +22,9 @@ ERROR_NAMES = {
 EXFEM_WAVE_P = 1
 EXFEM_WAVE_SV = 2
 
+EXFEM_POINT_FORCE = 1
+EXFEM_POINT_DISP = 2
+
 EXFEM_FP64 = 0
 EXFEM_FP32_KAHAN = 1
 
@@ -60,7 +63,9 @@ class Problem(C.Structure):
                 ("walpha", C.c_double), ("wbeta", C.c_double),
                 ("nrhs", C.c_int), ("waves", C.POINTER(Wave)),
                 ("nrecv", C.c_int), ("recv_xy", C.POINTER(C.c_double)),
-                ("recv_elem", C.POINTER(C.c_int))]
+                ("recv_elem", C.POINTER(C.c_int)),
+                ("point_kind", C.c_int), ("npoint", C.c_int), ("point_nodes", C.POINTER(C.c_int)),
+                ("point_amp", C.c_double), ("point_sigma", C.c_double), ("point_t0", C.c_double)]
 
 
 class Opts(C.Structure):

@@ -14,6 +14,8 @@ Workloads (sizes at scale=1):
                          quadtree levels, +-10% log-normal heterogeneity, SV fc 5 Hz
   valley_batched         the valley mesh with 64 right-hand sides
   serving_stream         seeded canyon/valley requests with Poisson arrivals
+  point_source           POINTN/POINTD Ricker source (model.f90:1051-1078) on the
+                         rectangle or the refined canyon
 """
 from __future__ import annotations
 
@@ -108,6 +110,43 @@ def canyon(scale=1.0, steps=8000, radius=500.0, nperlen=25.0, waves=None, refine
                  [ROCK_HALFSPACE], rhs[0][0], pparams, geom="CANYON",
                  gparams=(width / 2, 0.0, radius), receivers=(0.0, width - dist, dist), rhs=rhs,
                  refine=(refine_levels, refine_band * max(scale, 0.25)))
+
+
+def point_source(scale=1.0, steps=4000, kind="POINTN", geom="NONE", amp=None, sigma=0.01, start=0.4,
+                 dist=None, point=None, save_every=4, refine_levels=2):
+    """A point source (POINTN force or POINTD displacement) on the y dof of
+    every node within `dist` of `point` (setup_point_source,
+    model.f90:1051-1078); pparams = (amp, sigma, start, dist, x, y).
+
+    geom "NONE": the homogeneous rectangle's mesh (15.625 m), source at the
+    middle of the surface.  geom "CANYON": the canyon with two REFINE levels
+    around the rim, source on the surface at the rim, where refined and
+    hanging nodes lie within `dist`.  No DRM layer, no free field."""
+    if geom == "NONE":
+        h = 15.625
+        ncol = max(8, int(round(256 * scale)))
+        nrow = max(4, int(round(128 * scale)))
+        width, height = ncol * h, nrow * h
+        hmin, chper, nperlen, extra = h, 0.15625, 10, {}
+        point = point or (0.5 * width, 0.0)
+        dist = dist or 1.5 * h
+    else:
+        width, height = 6000.0 * scale, 3000.0 * scale
+        radius = 500.0 * scale
+        h = 10.0
+        hmin, chper, nperlen = h / 2 ** refine_levels, 0.25, 25
+        extra = dict(geom="CANYON", gparams=(width / 2, 0.0, radius),
+                     refine=(refine_levels, 60.0 * max(scale, 0.25)))
+        point = point or (width / 2 + radius + 0.5 * h, 0.0)
+        dist = dist or 3.0 * h
+    if amp is None:
+        amp = 1.0e6 if kind == "POINTN" else 1.0e-3
+    dt_bound = hmin / 4000.0   # dt = hmin/(vp*2) with vp 2000
+    ncol_r = 64
+    rd = width / ncol_r
+    return _deck(width, height, steps * dt_bound * 1.0000001, save_every * dt_bound, chper, nperlen, 2,
+                 [ROCK_HALFSPACE], kind, [amp, sigma, start, dist, point[0], point[1]],
+                 receivers=(0.0, width - rd, rd), **extra)
 
 
 VALLEY_MATERIALS = ["p 3000 s 1500 2400", "p 700 s 300 1800"]

@@ -106,7 +106,14 @@ class Model:
         return xy, el
 
     def waves(self):
+        """The right-hand sides' plane waves ([] for a point-source problem)."""
+        if not self.problem.waves:
+            return []
         return [self.problem.waves[i] for i in range(self.problem.nrhs)]
+
+    def point_nodes(self):
+        """1-based point-source nodes (setup_point_source), empty without one."""
+        return _arr(self.problem.point_nodes, self.problem.npoint, np.int32)
 
     def corners(self):
         """Non-hanging corners per element (elemallnhnodes), 1-based, shape (ne, 4)."""

@@ -15,6 +15,7 @@ SPECS = {
     "canyon": (decks.canyon, 8000, 4),
     "valley": (decks.valley, 20000, 10),
     "valley_batched": (decks.valley_batched, 20000, 10),
+    "point_source": (decks.point_source, 4000, 4),
 }
 
 

@@ -327,6 +327,10 @@ struct Model {
     std::vector<double> recv_xy;
     std::vector<int> recv_elem;
     std::vector<exfem_wave> waves;
+    // point source (setup_point_source): kind, Ricker parameters, 1-based nodes
+    int point_kind = 0;
+    double point_amp = 0, point_sigma = 0, point_t0 = 0, point_dist = 0;
+    std::vector<int> point_nodes;
     // exported 1-based mesh arrays
     std::vector<int> x_eptr, x_eind;
     std::vector<double> x_nodes;
@@ -347,6 +351,23 @@ struct Model {
         int c[4];
         corners(e, c);
         return ny[c[2]] - ny[c[0]];
+    }
+
+    // setup_point_source (model.f90:1051-1078): every node closer than the
+    // distance to one of the points (distance, utilities.f90:210-214), unique
+    // and in node order.
+    void setup_point_source() {
+        if (!point_kind) return;
+        const std::vector<double> &pp = deck.pparams;
+        std::vector<char> hit(nx.size(), 0);
+        for (size_t j = 4; j + 1 < pp.size(); j += 2)
+            for (size_t i = 0; i < nx.size(); ++i) {
+                double dx = pp[j] - nx[i], dy = pp[j + 1] - ny[i];
+                if (std::sqrt(dx * dx + dy * dy) < point_dist) hit[i] = 1;
+            }
+        point_nodes.clear();
+        for (size_t i = 0; i < nx.size(); ++i)
+            if (hit[i]) point_nodes.push_back((int)i + 1);
     }
 
     // inside_soil (model.f90:217-235): outside the DRM box
@@ -933,8 +954,20 @@ int build(const char *text, Model &m) {
             w.amp = m.deck.pparams[7]; w.freq = m.deck.pparams[8];
             m.waves.push_back(w);
         }
+    } else if (m.deck.prob == "POINTN" || m.deck.prob == "POINTD") {
+        // setup_point_source (model.f90:1051-1078): pparams = (amplitude,
+        // sigma, start time, distance, x1, y1, x2, y2, ...)
+        const std::vector<double> &pp = m.deck.pparams;
+        if (pp.size() < 6) return fail(EXFEM_E_ARG, "PROBLEM: POINTN/POINTD need amplitude, sigma, start, distance and a point");
+        if (!(pp[1] > 0)) return fail(EXFEM_E_ARG, "PROBLEM: point source sigma must be positive");
+        m.point_kind = (m.deck.prob == "POINTN") ? EXFEM_POINT_FORCE : EXFEM_POINT_DISP;
+        m.point_amp = pp[0];
+        m.point_sigma = pp[1];
+        m.point_t0 = pp[2];
+        m.point_dist = pp[3];
+        if (m.deck.have_rhs) return fail(EXFEM_E_ARG, "RHS: right-hand sides are plane waves; a point-source problem has one");
     } else {
-        return fail(EXFEM_E_UNSUPPORTED, "PROBLEM: only plane-wave (WAVEP/WAVESV) problems are on the accelerated path");
+        return fail(EXFEM_E_UNSUPPORTED, "PROBLEM: only WAVEP, WAVESV, POINTN and POINTD are on the accelerated path");
     }
     m.initial_mesh();
     // explicit.f90:42-52: cut, (redistribute: no-op on one rank), divide
@@ -950,6 +983,7 @@ int build(const char *text, Model &m) {
     m.setup_hanging();
     m.create_absorbingbc();
     m.wave_elems();
+    m.setup_point_source();
     m.apply_heterogeneity();
     m.recalculate_deltat();
     if (m.io_interval < 1) return fail(EXFEM_E_ARG, "TIME: save interval shorter than the time step");
@@ -1017,8 +1051,14 @@ void exfem_model_views(const exfem_model *m, exfem_mesh *mesh, exfem_problem *pr
         prob->wbox[2] = m->wtop;
         prob->walpha = m->walpha;
         prob->wbeta = m->wbeta;
-        prob->nrhs = (int)m->waves.size();
-        prob->waves = m->waves.data();
+        prob->nrhs = std::max(1, (int)m->waves.size());
+        prob->waves = m->waves.empty() ? nullptr : m->waves.data();
+        prob->point_kind = m->point_kind;
+        prob->npoint = (int)m->point_nodes.size();
+        prob->point_nodes = m->point_nodes.empty() ? nullptr : m->point_nodes.data();
+        prob->point_amp = m->point_amp;
+        prob->point_sigma = m->point_sigma;
+        prob->point_t0 = m->point_t0;
         prob->nrecv = (int)m->recv_elem.size();
         prob->recv_xy = m->recv_xy.data();
         prob->recv_elem = m->recv_elem.data();
@@ -1036,7 +1076,7 @@ void exfem_model_get_info(const exfem_model *m, exfem_model_info *info) {
     info->nmat_base = m->nmat_base; info->nmat = (int)(m->matconst.size() / 5);
     info->nelems = m->ne(); info->nnodes = (int)m->nx.size();
     info->nhanging = (int)(m->hanging.size() / 3); info->nseismic = (int)(m->seismic.size() / 2);
-    info->nrecv = (int)m->recv_elem.size(); info->nrhs = (int)m->waves.size();
+    info->nrecv = (int)m->recv_elem.size(); info->nrhs = std::max(1, (int)m->waves.size());
     info->nsteps = m->nsteps; info->io_interval = m->io_interval; info->deltat = m->deltat;
     info->nlevels = m->nlevels; info->min_h = m->min_h; info->max_h = m->max_h;
 }

@@ -99,7 +99,26 @@ typedef struct exfem_problem {
     int           nrecv;
     const double *recv_xy;    /* [2*nrecv] receiver points (find_highest output)    */
     const int    *recv_elem;  /* [nrecv] 1-based top element of each receiver       */
+    /* Point source (setup_point_source, model.f90:1051-1078).  The y dof of
+     * every listed node takes r(t) = amp exp(-t^2/(4 sigma)) (t^2 - 2 sigma) /
+     * (8 sqrt(pi) sigma^2.5) at t = time - t0 (ricker, formulation.f90:53-59):
+     *   EXFEM_POINT_FORCE (POINTN): added to the node's reaction after the
+     *     element sums, before the anchor sums (point_reactions,
+     *     model.f90:808-822; explicit.f90:144);
+     *   EXFEM_POINT_DISP (POINTD): set as its displacement after each update,
+     *     before the hanging-node averages, and at t = 0 and -dt for u and u-
+     *     (point_displacements, model.f90:831-845; explicit.f90:93-94, 150).
+     * Every right-hand side gets the same source.  Zero-initialised fields
+     * mean no point source.  A problem with a point source and no DRM layer
+     * (nseismic = 0) may pass waves = NULL: no free field is added anywhere. */
+    int           point_kind;  /* 0 (none), EXFEM_POINT_FORCE or EXFEM_POINT_DISP */
+    int           npoint;
+    const int    *point_nodes; /* [npoint] 1-based node ids (hanging ones allowed) */
+    double        point_amp, point_sigma, point_t0;   /* m_pointamp/sigma/start   */
 } exfem_problem;
+
+#define EXFEM_POINT_FORCE   1
+#define EXFEM_POINT_DISP    2
 
 typedef struct exfem_opts {
     int precision;     /* EXFEM_FP64 or EXFEM_FP32_KAHAN                          */

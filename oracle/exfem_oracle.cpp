@@ -237,6 +237,12 @@ void drm_mask(int bck, bool e[8]) {  // model.f90:778-793
     for (int i = 0; i < 8; ++i) e[i] = src ? src[i] : false;
 }
 
+// ricker (formulation.f90:53-59): the point-source pulse.
+double ricker_point(double amp, double sigma, double t) {
+    double r = std::exp(-(t * t) / (4 * sigma)) * (t * t - 2 * sigma) / (8 * std::sqrt(U_PI) * std::pow(sigma, 2.5));
+    return r * amp;
+}
+
 struct Solver {
     const exfem_mesh *mesh;
     const exfem_problem *prob;
@@ -247,8 +253,10 @@ struct Solver {
     double mmat[64];
     std::vector<double> mfull, u, up, ro;
     PWave wave;
+    bool have_wave = true;   // false: no plane wave (point-source problems), no free field
     double t0 = 0;
     int hang_mode = EXFEM_HANG_HALF;
+    std::vector<int> pdofs;  // y dof (0-based) of each point-source node, unique
 
     // elemallnhnodes (1-based node ids)
     inline void elemallnhnodes(int ele, int nodes[4]) const {
@@ -372,7 +380,7 @@ struct Solver {
                 fx = fx + inter[k] * u[dofs[2 * k] - 1];
                 fy = fy + inter[k] * u[dofs[2 * k + 1] - 1];
             }
-            if (inside_soil(px, py)) {
+            if (have_wave && inside_soil(px, py)) {
                 double d6[2][3];
                 planewave(wave, time - t0, px - prob->worigin[0], py - prob->worigin[1], d6);
                 fx = fx + d6[0][0];
@@ -444,14 +452,38 @@ int oracle_run(const exfem_mesh *mesh, const exfem_problem *prob, int rhs, int h
         for (int j = mesh->eptr[e] - 1; j < mesh->eptr[e + 1] - 1; ++j) cnt += !mesh->ediv[j];
         if (cnt != 4) { g_err = "element " + std::to_string(e + 1) + " has " + std::to_string(cnt) + " non-hanging nodes"; return EXFEM_E_MESH; }
     }
-    const exfem_wave &wv = prob->waves[rhs];
-    int rc = initplanewaves(S.wave, wv.kind, wv.amp, prob->walpha, prob->wbeta, wv.angle, wv.freq);
-    if (rc) return rc;
-    S.t0 = wv.t0;
+    if (prob->waves) {
+        const exfem_wave &wv = prob->waves[rhs];
+        int rc = initplanewaves(S.wave, wv.kind, wv.amp, prob->walpha, prob->wbeta, wv.angle, wv.freq);
+        if (rc) return rc;
+        S.t0 = wv.t0;
+    } else if (prob->nseismic > 0) {
+        g_err = "a DRM layer needs waves";
+        return EXFEM_E_ARG;
+    } else {
+        S.have_wave = false;
+    }
     const int ndof = 2 * S.nn;
+    // setup_point_source (model.f90:1051-1078): unique point nodes
+    const int pkind = prob->point_kind;
+    if (pkind != 0) {
+        std::vector<char> flag(S.nn, 0);
+        for (int i = 0; i < prob->npoint; ++i) {
+            int g = prob->point_nodes[i];
+            if (g < 1 || g > S.nn) { g_err = "point source node out of range"; return EXFEM_E_ARG; }
+            flag[g - 1] = 1;
+        }
+        for (int n = 0; n < S.nn; ++n)
+            if (flag[n]) S.pdofs.push_back(2 * n + 1);
+    }
+    const double pamp = prob->point_amp, psig = prob->point_sigma, pt0 = prob->point_t0;
     // init_explicit (explicit.f90:79-109)
     S.u.assign(ndof, 0.0);
     S.up.assign(ndof, 0.0);
+    if (pkind == EXFEM_POINT_DISP) {   // problem_displacements at 0 and -dt (explicit.f90:93-94)
+        for (int d : S.pdofs) S.u[d] = ricker_point(pamp, psig, 0.0 - pt0);
+        for (int d : S.pdofs) S.up[d] = ricker_point(pamp, psig, -S.dt - pt0);
+    }
     S.mfull.assign(ndof, 0.0);
     S.ro.assign(ndof, 0.0);
     for (int i = 0; i < S.ne; ++i) {
@@ -517,9 +549,13 @@ int oracle_run(const exfem_mesh *mesh, const exfem_problem *prob, int rhs, int h
                 S.ro[d] = acc;
             }
         }
+        if (pkind == EXFEM_POINT_FORCE)              // absolute_reactions (explicit.f90:144)
+            for (int d : S.pdofs) S.ro[d] = S.ro[d] + ricker_point(pamp, psig, (double)i * S.dt - pt0);
         S.sum_reactanchors(S.ro);                    // explicit.f90:145
         S.up.swap(S.u);                              // e_up = e_u (147)
         for (int d = 0; d < ndof; ++d) S.u[d] = S.ro[d] / S.mfull[d];   // (148)
+        if (pkind == EXFEM_POINT_DISP)               // problem_displacements (explicit.f90:150)
+            for (int d : S.pdofs) S.u[d] = ricker_point(pamp, psig, (double)i * S.dt - pt0);
         S.set_dispshanging(S.u);                     // (151)
         if (seis_out && i % io == 0) S.sample(i / io, seis, nrecv);
         if (!std::isfinite(S.u[0])) { /* keep going: callers inspect the output */ }

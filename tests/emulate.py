@@ -201,8 +201,8 @@ def emulate_fp32(model, nsteps, rhs=0, comp="bf16"):
         np.add.at(acc, t_node, -t_w[:, None] * np.stack([fx[t_e, t_c], fy[t_e, t_c]], axis=1))
         acc += E[:na] * dh[:na]
         if llist.size:
-            h, b = llist[:, 0], llist[:, 1]
-            term = f32(0.5) * (E[h] * dh[h] + D[h] * (f32(0.5) * (uh[b] - uh[l_node]) + (dh[h] - dh[l_node])))
+            h = llist[:, 0]
+            term = f32(0.5) * (E[h] * dh[h] + D[h] * ((uh[h] - uh[l_node]) + (dh[h] - dh[l_node])))
             np.add.at(acc, l_node, term.astype(f32))
         delta = (acc * inv_m).astype(f32)
         # D+ = D + delta (Kahan, compensation rounded to `comp`)

@@ -134,7 +134,7 @@ def test_tile_halo_slots_point_at_the_right_nodes(tn):
     assert np.array_equal(hlist[hptr[node_tile] + nslot], np.arange(na))
     link_node = np.repeat(np.arange(na), np.diff(P.lptr))
     if link_node.size:
-        assert np.array_equal(hlist[hptr[node_tile[link_node]] + lslot], P.llist.reshape(-1, 2)[:, 1])
+        assert np.array_equal(hlist[hptr[node_tile[link_node]] + lslot], P.llist.reshape(-1, 2)[:, 0])
 
 
 def _u16(a):
