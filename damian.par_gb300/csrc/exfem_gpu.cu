@@ -14,6 +14,7 @@
 //               the in-loop receiver samples (visu_field) on save steps
 // The step counter lives on the device so a captured CUDA graph of several
 // steps can be replayed unchanged.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -193,6 +194,42 @@ __global__ void k_point_set64(DevModel m, double *u, double v) {
     if (t >= (long long)m.npoint * m.R) return;
     const int n = m.pnodes[t / m.R], r = (int)(t % m.R);
     u[((size_t)n * 2 + 1) * m.R + r] = v;
+}
+
+// visu_field at arbitrary points: FP64 rows (u64) or FP32 hi - comp (uh, uc).
+__global__ void k_sample_points(DevModel m, const double *__restrict__ u64, const float *__restrict__ uh,
+                                const unsigned short *__restrict__ uc, int rhs, int np, const int *__restrict__ node,
+                                const double *__restrict__ w, const int *__restrict__ soil,
+                                const double *__restrict__ xy, double time, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const size_t R = m.R;
+    double fx = 0.0, fy = 0.0;
+    if (node[4 * (size_t)i] >= 0) {
+        for (int k = 0; k < 4; ++k) {
+            const size_t b = ((size_t)node[4 * (size_t)i + k] * 2) * R + rhs;
+            double vx, vy;
+            if (u64) {
+                vx = u64[b];
+                vy = u64[b + R];
+            } else {
+                vx = (double)uh[b] - (double)__bfloat162float(__ushort_as_bfloat16(uc[b]));
+                vy = (double)uh[b + R] - (double)__bfloat162float(__ushort_as_bfloat16(uc[b + R]));
+            }
+            const double wk = w[4 * (size_t)i + k];
+            fx = fx + wk * vx;
+            fy = fy + wk * vy;
+        }
+        if (soil[i]) {
+            const DevWave wv = m.waves[rhs];
+            double dx, dz;
+            planewave_u(wv, time - wv.t0, xy[2 * (size_t)i] - m.worigin_x, xy[2 * (size_t)i + 1] - m.worigin_y, dx, dz);
+            fx = fx + dx;
+            fy = fy + dz;
+        }
+    }
+    out[2 * (size_t)i] = fx;
+    out[2 * (size_t)i + 1] = fy;
 }
 
 int launch_step64(Ctx &c, int par) {
@@ -669,6 +706,50 @@ int exfem_gpu_profile_kernels(exfem_ctx *ctx, int nsteps, double *ms_out, const 
         names_out[k] = keep[k].c_str();
     }
     return n;
+}
+
+int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *xy, const int *elem, double *out) {
+    if (!ctx) return EXFEM_E_ARG;
+    Ctx &c = *ctx;
+    if (!c.inited) { c.err = "exfem_gpu_sample_points before exfem_gpu_init_explicit"; return EXFEM_E_STATE; }
+    if (rhs < 0 || rhs >= c.plan.R || npoint < 0 || (npoint > 0 && (!xy || !elem || !out))) {
+        c.err = "bad sample_points arguments";
+        return EXFEM_E_ARG;
+    }
+    if (npoint == 0) return EXFEM_OK;
+    std::vector<int> node, soil;
+    std::vector<double> w;
+    if (int rc = point_weights(c.plan, npoint, xy, elem, node, w, soil, c.err)) return rc;
+    CK(cudaSetDevice(c.device));
+    // one scratch block: corners, soil flags, weights, points, output
+    const size_t n = (size_t)npoint;
+    const size_t bytes = n * (16 + 4) + n * (32 + 16 + 16) + 64;
+    void *buf = nullptr;
+    CK(cudaMalloc(&buf, bytes));
+    char *b = static_cast<char *>(buf);
+    double *d_w = reinterpret_cast<double *>(b);
+    double *d_xy = d_w + 4 * n;
+    double *d_out = d_xy + 2 * n;
+    int *d_node = reinterpret_cast<int *>(d_out + 2 * n);
+    int *d_soil = d_node + 4 * n;
+    cudaError_t e = cudaMemcpyAsync(d_w, w.data(), 32 * n, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_xy, xy, 16 * n, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_node, node.data(), 16 * n, cudaMemcpyHostToDevice, c.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_soil, soil.data(), 4 * n, cudaMemcpyHostToDevice, c.stream);
+    const double time = c.plan.dt * (double)c.steps_done;
+    if (e == cudaSuccess) {
+        const bool f64 = c.precision == EXFEM_FP64;
+        k_sample_points<<<nblocks((long long)npoint, 128), 128, 0, c.stream>>>(
+            c.dm, f64 ? c.u64[c.parity] : nullptr, f64 ? nullptr : c.uhi[c.parity], f64 ? nullptr : c.ucomp, rhs,
+            npoint, d_node, d_w, d_soil, d_xy, time, d_out);
+        c.launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, 16 * n, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) { c.err = std::string("sample_points: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    return EXFEM_OK;
 }
 
 int exfem_gpu_steps_done(const exfem_ctx *ctx) { return ctx ? ctx->steps_done : 0; }

@@ -413,34 +413,26 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         P.dlist.insert(P.dlist.end(), dl[n].begin(), dl[n].end());
         P.dptr[n + 1] = (int)P.dlist.size();
     }
+    // ---- kept for point sampling
+    P.elem_of_ref = elem_of_ref;
+    P.nxy.resize(2 * (size_t)nn);
+    for (int i = 0; i < nn; ++i) {
+        P.nxy[2 * (size_t)P.node_of_ref[i]] = xs[i];
+        P.nxy[2 * (size_t)P.node_of_ref[i] + 1] = ys[i];
+    }
+    for (int k = 0; k < 3; ++k) P.wbox[k] = prob.wbox[k];
+    P.have_waves = prob.waves != nullptr;
     // ---- receivers (visu_field, visualization.f90:156-181)
     P.nrecv = prob.nrecv;
-    P.rnode.assign((size_t)4 * P.nrecv, 0);
-    P.rw.assign((size_t)4 * P.nrecv, 0.0);
-    P.rsoil.assign(P.nrecv, 0);
     P.rxy.assign((size_t)2 * P.nrecv, 0.0);
+    if (P.nrecv > 0) std::copy(prob.recv_xy, prob.recv_xy + 2 * (size_t)P.nrecv, P.rxy.begin());
     for (int i = 0; i < P.nrecv; ++i) {
-        int e = prob.recv_elem[i] - 1;
-        if (e < 0 || e >= ne) { err = "receiver " + std::to_string(i + 1) + " element out of range"; return EXFEM_E_ARG; }
-        double px = prob.recv_xy[2 * i], py = prob.recv_xy[2 * i + 1];
-        const int *c = &corner_ref[(size_t)e * 4];
-        // shapeparams (formulation.f90:334-343) and shapefuncs (356-363)
-        double r = (px - xs[c[0]]) / (xs[c[2]] - xs[c[0]]);
-        double s = (py - ys[c[0]]) / (ys[c[2]] - ys[c[0]]);
-        r = 2.0 * r - 1.0; s = 2.0 * s - 1.0;
-        r = std::min(1.0, std::max(-1.0, r)); s = std::min(1.0, std::max(-1.0, s));
-        double inter[4] = {(1 - r) * (1 - s) / 4, (1 + r) * (1 - s) / 4, (1 + r) * (1 + s) / 4, (1 - r) * (1 + s) / 4};
-        for (int k = 0; k < 4; ++k) {
-            P.rnode[(size_t)4 * i + k] = P.node_of_ref[c[k]];
-            P.rw[(size_t)4 * i + k] = inter[k];
-        }
-        P.rsoil[i] = realunder(px, prob.wbox[0]) || realover(px, prob.wbox[1]) || realover(py, prob.wbox[2]);
-        P.rxy[2 * i] = px;
-        P.rxy[2 * i + 1] = py;
+        const int e = prob.recv_elem[i];
+        if (e < 1 || e > ne) { err = "receiver " + std::to_string(i + 1) + " element out of range"; return EXFEM_E_ARG; }
     }
+    if (int rc = point_weights(P, P.nrecv, prob.recv_xy, prob.recv_elem, P.rnode, P.rw, P.rsoil, err)) return rc;
     // ---- waves (none: zero amplitudes, and no receiver adds a free field)
     P.waves.resize(P.R);
-    P.have_waves = prob.waves != nullptr;
     for (int r = 0; r < P.R; ++r) {
         if (!prob.waves) {
             P.waves[r] = WaveConst();
@@ -452,7 +444,6 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         int rc = init_wave_const(prob.waves[r], prob.walpha, prob.wbeta, P.waves[r], err);
         if (rc) { err = "rhs " + std::to_string(r) + ": " + err; return rc; }
     }
-    if (!prob.waves) P.rsoil.assign(P.nrecv, 0);
     // ---- point source: flags on internal nodes
     P.point_kind = prob.point_kind;
     P.point_amp = prob.point_amp;
@@ -465,6 +456,36 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             if (g < 1 || g > nn) { err = "point source node out of range"; return EXFEM_E_ARG; }
             P.pflag[P.node_of_ref[g - 1]] = 1;
         }
+    }
+    return EXFEM_OK;
+}
+
+int point_weights(const Plan &P, int npt, const double *xy, const int *elem, std::vector<int> &node,
+                  std::vector<double> &w, std::vector<int> &soil, std::string &err) {
+    node.assign(4 * (size_t)std::max(npt, 0), -1);
+    w.assign(4 * (size_t)std::max(npt, 0), 0.0);
+    soil.assign(std::max(npt, 0), 0);
+    for (int i = 0; i < npt; ++i) {
+        const int e = elem[i];
+        if (e == 0) continue;
+        if (e < 1 || e > P.ne) { err = "point " + std::to_string(i + 1) + " element out of range"; return EXFEM_E_ARG; }
+        const int ie = P.elem_of_ref[e - 1];
+        const int *c = &P.econn[(size_t)ie * 4];
+        const double px = xy[2 * (size_t)i], py = xy[2 * (size_t)i + 1];
+        const double x0 = P.nxy[2 * (size_t)c[0]], y0 = P.nxy[2 * (size_t)c[0] + 1];
+        const double x2 = P.nxy[2 * (size_t)c[2]], y2 = P.nxy[2 * (size_t)c[2] + 1];
+        // shapeparams (formulation.f90:334-343) and shapefuncs (356-363)
+        double r = (px - x0) / (x2 - x0);
+        double s = (py - y0) / (y2 - y0);
+        r = 2.0 * r - 1.0; s = 2.0 * s - 1.0;
+        r = std::min(1.0, std::max(-1.0, r)); s = std::min(1.0, std::max(-1.0, s));
+        const double inter[4] = {(1 - r) * (1 - s) / 4, (1 + r) * (1 - s) / 4, (1 + r) * (1 + s) / 4,
+                                 (1 - r) * (1 + s) / 4};
+        for (int k = 0; k < 4; ++k) {
+            node[4 * (size_t)i + k] = c[k];
+            w[4 * (size_t)i + k] = inter[k];
+        }
+        soil[i] = P.have_waves && (realunder(px, P.wbox[0]) || realover(px, P.wbox[1]) || realover(py, P.wbox[2]));
     }
     return EXFEM_OK;
 }

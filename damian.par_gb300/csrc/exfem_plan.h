@@ -66,6 +66,11 @@ struct Plan {
     std::vector<int> rsoil;
     std::vector<double> rxy;
     int nrecv = 0;
+    // kept for point sampling after setup: reference -> internal element,
+    // internal node coordinates, the DRM box (left, right, top)
+    std::vector<int> elem_of_ref;
+    std::vector<double> nxy;
+    double wbox[3] = {0, 0, 0};
     // waves (have_waves false: zero-amplitude placeholders, no free field)
     std::vector<WaveConst> waves;
     bool have_waves = true;
@@ -82,6 +87,14 @@ struct Plan {
     // own DRM incidences of every node: slot*4+corner in seismic order
     std::vector<int> odptr, odlist;
 };
+
+// visu_field's interpolation data (visualization.f90:156-181) for npt points
+// in 1-based reference elements: the element's 4 corners (internal ids), the
+// shapefuncs weights at the clamped local coordinates (shapeparams,
+// formulation.f90:315-363) and inside_soil (0 without waves).  elem 0 marks a
+// point outside the mesh: corners -1, weights 0.
+int point_weights(const Plan &P, int npt, const double *xy, const int *elem, std::vector<int> &node,
+                  std::vector<double> &w, std::vector<int> &soil, std::string &err);
 
 // Shared-memory tiles of the FP32 step: consecutive active nodes (Morton
 // order, so a tile is a compact patch) and the halo of nodes their terms read.

@@ -123,6 +123,8 @@ GPU_SYMBOLS = {
     "exfem_gpu_get_u": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t]),
     "exfem_gpu_get_seismograms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_size_t,
                                             C.POINTER(C.c_int)]),
+    "exfem_gpu_sample_points": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "exfem_gpu_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "exfem_gpu_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                             C.POINTER(C.c_char_p), C.c_int]),
@@ -135,6 +137,13 @@ GPU_SYMBOLS = {
     "exfem_gpu_destroy": (None, [C.c_void_p]),
 }
 
+class Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("origin", C.c_double * 2), ("space", C.c_double),
+                ("npoints", C.c_int), ("points", C.POINTER(C.c_double)), ("elem", C.POINTER(C.c_int)),
+                ("material", C.POINTER(C.c_double)), ("ncells", C.c_int), ("eptr", C.POINTER(C.c_int)),
+                ("eind", C.POINTER(C.c_int)), ("nfound", C.c_int)]
+
+
 HOST_SYMBOLS = {
     "exfem_model_build": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
     "exfem_model_error": (C.c_char_p, []),
@@ -146,6 +155,11 @@ HOST_SYMBOLS = {
     "exfem_write_step": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "exfem_write_sheet": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_double), C.c_int,
                                     C.POINTER(C.c_double), C.c_double]),
+    "exfem_model_grid": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.POINTER(C.POINTER(Grid))]),
+    "exfem_grid_free": (None, [C.POINTER(Grid)]),
+    "exfem_write_vtu": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
+                                  C.POINTER(C.c_double), C.c_char_p, C.POINTER(C.c_double)]),
     "exfem_model_free": (None, [C.c_void_p]),
 }
 

@@ -101,6 +101,16 @@ class Solver:
             self._check(nk)
         return {nm[i].decode(): ms[i] for i in range(nk)}
 
+    def sample_points(self, xy, elem, rhs=0):
+        """visu_field at points (n, 2) in 1-based elements (0: none) for the
+        current step: (n, 2) displacements."""
+        pts = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        el = np.ascontiguousarray(elem, dtype=np.int32)
+        out = np.zeros((pts.shape[0], 2))
+        self._check(self.lib.exfem_gpu_sample_points(self.h, int(rhs), pts.shape[0], _dp(pts),
+                                                     el.ctypes.data_as(C.POINTER(C.c_int)), _dp(out)))
+        return out
+
     def u(self, rhs=0):
         out = np.zeros(2 * self.model.nnodes)
         self._check(self.lib.exfem_gpu_get_u(self.h, int(rhs), _dp(out), out.size))

@@ -11,7 +11,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native
-from .abi import (HOST_SYMBOLS, ExfemError, Mesh, ModelInfo, Problem, bind)
+from .abi import (HOST_SYMBOLS, ExfemError, Grid, Mesh, ModelInfo, Problem, bind)
 
 _host = None
 
@@ -124,6 +124,28 @@ class Model:
             raise ExfemError(-2, "element without four non-hanging corners")
         return eind[keep].reshape(-1, 4)
 
+    def grid(self, xmin, xmax, ymin, ymax, dist):
+        """ANIMAT sampling grid (exfem_model_grid): dict with nx, ny, points
+        (n, 2), elem (n,) 1-based or 0, material (n, 2), eptr, eind (1-based
+        cells) and nfound."""
+        g = C.POINTER(Grid)()
+        rc = host_lib().exfem_model_grid(self._h, float(xmin), float(xmax), float(ymin), float(ymax), float(dist),
+                                         C.byref(g))
+        if rc != 0:
+            raise ExfemError(rc, host_lib().exfem_model_error().decode())
+        try:
+            v = g.contents
+            n, nc = v.npoints, v.ncells
+            out = {"nx": v.nx, "ny": v.ny, "origin": (v.origin[0], v.origin[1]), "space": v.space,
+                   "points": _arr(v.points, 2 * n, np.float64).reshape(-1, 2).copy(),
+                   "elem": _arr(v.elem, n, np.int32).copy(),
+                   "material": _arr(v.material, 2 * n, np.float64).reshape(-1, 2).copy(),
+                   "eptr": _arr(v.eptr, nc + 1, np.int32).copy(),
+                   "eind": _arr(v.eind, 4 * nc, np.int32).copy(), "nfound": v.nfound}
+        finally:
+            host_lib().exfem_grid_free(g)
+        return out
+
     # ---- reference file formats --------------------------------------------
     def save_mesh(self, path):
         rc = host_lib().exfem_model_save_mesh(self._h, str(path).encode())
@@ -159,5 +181,20 @@ def write_sheet(path, points, field, samp):
     rc = host_lib().exfem_write_sheet(str(path).encode(), pts.shape[0],
                                       pts.ctypes.data_as(C.POINTER(C.c_double)), fld.shape[0],
                                       fld.ctypes.data_as(C.POINTER(C.c_double)), float(samp))
+    if rc != 0:
+        raise ExfemError(rc, host_lib().exfem_model_error().decode())
+
+
+def write_vtu(path, eptr, eind, points, field, name="displacements"):
+    """VTK unstructured grid of write_vtk_unst_field (io.cpp:699-842):
+    points (n, 2), field (n, 2), 1-based cells eptr/eind."""
+    ep = np.ascontiguousarray(eptr, dtype=np.int32)
+    ei = np.ascontiguousarray(eind, dtype=np.int32)
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    fld = np.ascontiguousarray(field, dtype=np.float64)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    rc = host_lib().exfem_write_vtu(str(path).encode(), len(ep) - 1, ip(ep), ip(ei), pts.shape[0], dp(pts),
+                                    name.encode(), dp(fld))
     if rc != 0:
         raise ExfemError(rc, host_lib().exfem_model_error().decode())

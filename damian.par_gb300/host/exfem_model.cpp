@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <new>
 #include <random>
 #include <sstream>
 #include <string>
@@ -995,6 +996,150 @@ int build(const char *text, Model &m) {
 template <typename T>
 bool fwrite_all(FILE *f, const T *p, size_t n) { return std::fwrite(p, sizeof(T), n, f) == n; }
 
+// ---------------------------------------------------- element quadtree ----
+// Restatement of order_quadtree/search_quadtree (quadtree.f90:21-251):
+// nodes split their elements about a centre snapped to the base length (or
+// to the halved length that still fits the box), left/right by the lower
+// x corner and down/up by the lower y corner; a leaf holds one element.
+inline double realfloor(double a) { return std::floor(a + U_TOL); }      // utilities.f90:177-181
+inline double realceiling(double a) { return std::ceil(a - U_TOL); }     // utilities.f90:183-187
+
+struct QTree {
+    struct Node {
+        double cx = 0, cy = 0;
+        int elem = -1;                 // 0-based leaf element, -1 inner node
+        int child[4] = {-1, -1, -1, -1};   // downleft, upleft, downright, upright
+    };
+    std::vector<Node> nodes;
+    const Model *m = nullptr;
+
+    void box(int e, double &x0, double &y0, double &x1, double &y1) const {
+        int c[4];
+        m->corners(e, c);
+        x0 = m->nx[c[0]]; y0 = m->ny[c[0]]; x1 = m->nx[c[2]]; y1 = m->ny[c[2]];
+    }
+    // pivot split of elems[lo, hi) by the lower corner against centre v (axis 0 = x)
+    int split(std::vector<int> &el, int lo, int hi, int axis, double v) const {
+        int st = lo, en = hi - 1;
+        while (st <= en) {
+            double a0, b0, a1, b1, c0, d0, c1, d1;
+            box(el[st], a0, b0, a1, b1);
+            box(el[en], c0, d0, c1, d1);
+            if (realover(v, axis == 0 ? a0 : b0)) { ++st; continue; }
+            if (realunder(v, axis == 0 ? c1 : d1)) { --en; continue; }
+            std::swap(el[st], el[en]);
+            ++st;
+            --en;
+        }
+        return st;
+    }
+    int build(std::vector<int> &el, int lo, int hi, int depth) {
+        const int id = (int)nodes.size();
+        nodes.emplace_back();
+        if (hi - lo == 1 || depth > 200) { nodes[id].elem = el[lo]; return id; }
+        const double inf = std::numeric_limits<double>::infinity();
+        double mn[2] = {inf, inf}, mx[2] = {-inf, -inf};
+        for (int i = lo; i < hi; ++i) {
+            double x0, y0, x1, y1;
+            box(el[i], x0, y0, x1, y1);
+            mn[0] = std::min(mn[0], x0); mn[1] = std::min(mn[1], y0);
+            mx[0] = std::max(mx[0], x1); mx[1] = std::max(mx[1], y1);
+        }
+        double dist[2] = {mx[0] - mn[0], mx[1] - mn[1]};
+        const double bl = m->blength;
+        double len = bl;
+        if (!(realunder(bl, dist[0]) || realunder(bl, dist[1]))) {
+            len = bl / 2.0;
+            while (!realunder(len, dist[0]) && !realunder(len, dist[1])) len = len / 2.0;
+        }
+        for (int a = 0; a < 2; ++a) {
+            mn[a] = realfloor(mn[a] / len) * len;
+            mx[a] = realceiling(mx[a] / len) * len;
+            dist[a] = realfloor(((mx[a] - mn[a]) / 2.0) / len) * len;
+        }
+        const double cx = mn[0] + dist[0], cy = mn[1] + dist[1];
+        nodes[id].cx = cx;
+        nodes[id].cy = cy;
+        const int mid = split(el, lo, hi, 0, cx);
+        if (mid > lo) {
+            const int s = split(el, lo, mid, 1, cy);
+            if (s > lo) { int k = build(el, lo, s, depth + 1); nodes[id].child[0] = k; }
+            if (s < mid) { int k = build(el, s, mid, depth + 1); nodes[id].child[1] = k; }
+        }
+        if (mid < hi) {
+            const int s = split(el, mid, hi, 1, cy);
+            if (s > mid) { int k = build(el, mid, s, depth + 1); nodes[id].child[2] = k; }
+            if (s < hi) { int k = build(el, s, hi, depth + 1); nodes[id].child[3] = k; }
+        }
+        return id;
+    }
+    void build(const Model &model) {
+        m = &model;
+        nodes.clear();
+        std::vector<int> el(model.ne());
+        for (int e = 0; e < model.ne(); ++e) el[e] = e;
+        if (!el.empty()) build(el, 0, (int)el.size(), 0);
+    }
+    // inside_element (model.f90:176-186)
+    bool inside(int e, double px, double py) const {
+        double x0, y0, x1, y1;
+        box(e, x0, y0, x1, y1);
+        return !realunder(px, x0) && !realunder(py, y0) && !realover(px, x1) && !realover(py, y1);
+    }
+    // search_quadtree: 0-based element or -1
+    int search(double px, double py) const {
+        int t = nodes.empty() ? -1 : 0;
+        while (t >= 0) {
+            const Node &n = nodes[t];
+            if (n.elem >= 0) return inside(n.elem, px, py) ? n.elem : -1;
+            const bool ux = px < n.cx, uy = py < n.cy;
+            t = ux ? (uy ? n.child[0] : n.child[1]) : (uy ? n.child[2] : n.child[3]);
+        }
+        return -1;
+    }
+};
+
+// base64 of write_vtk_unst_field (io.cpp:623-663)
+const char B64[] = "ABCDEFGHIJKLMNOPQRSTUVWXYZabcdefghijklmnopqrstuvwxyz0123456789+/";
+
+std::string b64(const unsigned char *in, size_t n) {
+    std::string out;
+    out.reserve(4 * ((n + 2) / 3));
+    for (size_t i = 0; i < n;) {
+        unsigned a = i < n ? in[i++] : 0, b = i < n ? in[i++] : 0, c = i < n ? in[i++] : 0;
+        unsigned t = (a << 16) + (b << 8) + c;
+        out += B64[(t >> 18) & 63]; out += B64[(t >> 12) & 63]; out += B64[(t >> 6) & 63]; out += B64[t & 63];
+    }
+    static const int pad[3] = {0, 2, 1};
+    for (int i = 0; i < pad[n % 3]; ++i) out[out.size() - 1 - i] = '=';
+    return out;
+}
+
+// num_to_base64: the four little-endian bytes of an int as 8 characters
+std::string b64_len(int v) {
+    unsigned char ch[4];
+    std::memcpy(ch, &v, 4);
+    unsigned t = ((unsigned)ch[0] << 16) + ((unsigned)ch[1] << 8) + ch[2];
+    std::string out;
+    out += B64[(t >> 18) & 63]; out += B64[(t >> 12) & 63]; out += B64[(t >> 6) & 63]; out += B64[t & 63];
+    t = (unsigned)ch[3] << 16;
+    out += B64[(t >> 18) & 63]; out += B64[(t >> 12) & 63];
+    out += "==";
+    return out;
+}
+
+// pointdata_to_base64: (x, y) pairs as float (x, y, 0) triples
+std::string b64_points(int n, const double *p) {
+    std::vector<float> f((size_t)3 * n);
+    for (int i = 0; i < n; ++i) { f[3 * (size_t)i] = (float)p[2 * (size_t)i]; f[3 * (size_t)i + 1] = (float)p[2 * (size_t)i + 1]; f[3 * (size_t)i + 2] = 0.0f; }
+    return b64(reinterpret_cast<const unsigned char *>(f.data()), f.size() * sizeof(float));
+}
+
+struct Grid : exfem_grid {
+    std::vector<double> pts, mat;
+    std::vector<int> el, ptr, ind;
+};
+
 }  // namespace
 
 struct exfem_model : Model {};
@@ -1141,6 +1286,143 @@ int exfem_write_sheet(const char *path, int npoints, const double *points, int n
     std::fprintf(f, "SAMP = %lf ;", samp);
     std::fclose(f);
     return 0;
+}
+
+int exfem_model_grid(const exfem_model *m, double xmin, double xmax, double ymin, double ymax, double dist,
+                     exfem_grid **out) {
+    if (!m || !out || !(dist > 0) || !(xmax >= xmin) || !(ymax >= ymin)) return fail(EXFEM_E_ARG, "bad grid");
+    *out = nullptr;
+    // visu_points (visualization.f90:129-154)
+    const int nx = (int)((xmax - xmin) / dist), ny = (int)((ymax - ymin) / dist);
+    if ((double)(nx + 1) * (ny + 1) > 2.0e8) return fail(EXFEM_E_ARG, "grid over 2e8 points");
+    Grid *g = new (std::nothrow) Grid();
+    if (!g) return fail(EXFEM_E_NOMEM, "grid");
+    const int np = (nx + 1) * (ny + 1);
+    g->pts.resize(2 * (size_t)np);
+    int k = 0;
+    for (int i = 0; i <= nx; ++i)
+        for (int j = 0; j <= ny; ++j, ++k) {
+            g->pts[2 * (size_t)k] = xmin + (double)i * dist;
+            g->pts[2 * (size_t)k + 1] = ymin + (double)j * dist;
+        }
+    QTree qt;
+    qt.build(*m);
+    g->el.assign(np, 0);
+    g->mat.assign(2 * (size_t)np, 0.0);
+    int found = 0;
+    for (int p = 0; p < np; ++p) {
+        const double px = g->pts[2 * (size_t)p], py = g->pts[2 * (size_t)p + 1];
+        const int e = qt.search(px, py);
+        if (e < 0) continue;
+        g->el[p] = e + 1;
+        ++found;
+        const int prop = m->material_prop(px, py);   // visu_material
+        g->mat[2 * (size_t)p] = (double)prop;
+        g->mat[2 * (size_t)p + 1] = m->matconst[5 * (size_t)(prop - 1) + 3];
+    }
+    // create_struct_mesh (mesh_utils.f90:846-878)
+    g->ptr.assign((size_t)nx * ny + 1, 1);
+    g->ind.resize(4 * (size_t)nx * ny);
+    int c = 0;
+    for (int i = 1; i <= nx; ++i)
+        for (int j = 1; j <= ny; ++j, ++c) {
+            g->ptr[c + 1] = g->ptr[c] + 4;
+            int *q = &g->ind[4 * (size_t)c];
+            q[0] = (i - 1) * (ny + 1) + j;
+            q[1] = i * (ny + 1) + j;
+            q[2] = i * (ny + 1) + (j + 1);
+            q[3] = (i - 1) * (ny + 1) + (j + 1);
+        }
+    g->nx = nx; g->ny = ny;
+    g->origin[0] = xmin; g->origin[1] = ymin;
+    g->space = dist;
+    g->npoints = np;
+    g->points = g->pts.data();
+    g->elem = g->el.data();
+    g->material = g->mat.data();
+    g->ncells = nx * ny;
+    g->eptr = g->ptr.data();
+    g->eind = g->ind.data();
+    g->nfound = found;
+    *out = g;
+    return 0;
+}
+
+void exfem_grid_free(exfem_grid *g) { delete static_cast<Grid *>(g); }
+
+int exfem_write_vtu(const char *path, int ncells, const int *eptr, const int *eind, int npoints,
+                    const double *points, const char *fieldname, const double *field) {
+    if (!path || ncells < 0 || npoints < 0 || (ncells && (!eptr || !eind)) || (npoints && (!points || !field)) ||
+        !fieldname)
+        return fail(EXFEM_E_ARG, "bad vtu arguments");
+    FILE *f = std::fopen(path, "w");
+    if (!f) return fail(EXFEM_E_ARG, std::string("cannot open ") + path);
+    const int nconn = ncells ? eptr[ncells] - 1 : 0;
+    int off[6];
+    off[0] = 0;
+    off[1] = off[0] + 4 * (int)((((size_t)npoints * sizeof(float) * 3) + 2) / 3) + 8;
+    off[2] = off[1] + 4 * (int)((((size_t)npoints * sizeof(float) * 3) + 2) / 3) + 8;
+    off[3] = off[2] + 4 * (int)((((size_t)nconn * sizeof(int)) + 2) / 3) + 8;
+    off[4] = off[3] + 4 * (int)((((size_t)ncells * sizeof(int)) + 2) / 3) + 8;
+    off[5] = off[4] + 4 * (int)((((size_t)ncells * sizeof(int)) + 2) / 3) + 8;
+    std::fprintf(f, "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n");
+    std::fprintf(f, "<UnstructuredGrid>\n");
+    std::fprintf(f, "<Piece NumberOfPoints=\"%d\" NumberOfCells=\"%d\">\n", npoints, ncells);
+    std::fprintf(f, "<PointData>\n");
+    std::fprintf(f, "<DataArray type=\"Float32\" Name=\"%s\"", fieldname);
+    std::fprintf(f, " NumberOfComponents=\"3\" format=\"appended\" offset=\"%d\">\n", off[0]);
+    std::fprintf(f, "\n</DataArray>\n");
+    std::fprintf(f, "</PointData>\n");
+    std::fprintf(f, "<CellData>\n");
+    std::fprintf(f, "</CellData>\n");
+    std::fprintf(f, "<Points>\n");
+    std::fprintf(f, "<DataArray type=\"Float32\" Name=\"points\"");
+    std::fprintf(f, " NumberOfComponents=\"3\" format=\"appended\" offset=\"%d\">\n", off[1]);
+    std::fprintf(f, "\n</DataArray>\n");
+    std::fprintf(f, "</Points>\n");
+    std::fprintf(f, "<Cells>\n");
+    std::fprintf(f, "<DataArray type=\"Int32\" Name=\"connectivity\" format=\"appended\" offset=\"%d\">\n", off[2]);
+    std::fprintf(f, "\n</DataArray>\n");
+    std::fprintf(f, "<DataArray type=\"Int32\" Name=\"offsets\" Format=\"appended\" offset=\"%d\">\n", off[3]);
+    std::fprintf(f, "\n</DataArray>\n");
+    std::fprintf(f, "<DataArray type=\"Int32\" Name=\"types\" Format=\"appended\" offset=\"%d\">\n", off[4]);
+    std::fprintf(f, "\n</DataArray>\n");
+    std::fprintf(f, "</Cells>\n");
+    std::fprintf(f, "</Piece>\n");
+    std::fprintf(f, "</UnstructuredGrid>\n\n");
+    std::fprintf(f, "<AppendedData encoding=\"base64\">\n\n");
+    std::fputc('_', f);
+    // each block: its base64 length as an 8-character word, then the data
+    std::string t = b64_points(npoints, field);
+    std::fputs(b64_len((int)t.size()).c_str(), f);
+    std::fputs(t.c_str(), f);
+    t = b64_points(npoints, points);
+    std::fputs(b64_len((int)t.size()).c_str(), f);
+    std::fputs(t.c_str(), f);
+    // mesh_to_base64: 0-based connectivity, end offsets
+    std::vector<int> conn(nconn), offs(ncells);
+    for (int i = 0; i < ncells; ++i) {
+        offs[i] = eptr[i + 1] - 1;
+        for (int j = eptr[i] - 1; j < eptr[i + 1] - 1; ++j) conn[j] = eind[j] - 1;
+    }
+    t = b64(reinterpret_cast<const unsigned char *>(conn.data()), conn.size() * sizeof(int));
+    std::fputs(b64_len((int)t.size()).c_str(), f);
+    std::fputs(t.c_str(), f);
+    t = b64(reinterpret_cast<const unsigned char *>(offs.data()), offs.size() * sizeof(int));
+    const std::string offlen = b64_len((int)t.size());
+    std::fputs(offlen.c_str(), f);
+    std::fputs(t.c_str(), f);
+    // types: the offsets' length word again, then VTK_POLYGON (7) in groups
+    // of three cells plus the remainder, as io.cpp:827-833 writes them
+    std::fputs(offlen.c_str(), f);
+    for (int i = 0; i < ncells; i += 3) std::fputs("BwAAAAcAAAAHAAAA", f);
+    if (ncells % 3 == 1) std::fputs("BwAAAA==", f);
+    else if (ncells % 3 == 2) std::fputs("BwAAAAcAAAA=", f);
+    std::fprintf(f, "\n\n</AppendedData>\n");
+    std::fprintf(f, "</VTKFile>\n");
+    const bool ok = std::ferror(f) == 0;
+    std::fclose(f);
+    return ok ? 0 : fail(EXFEM_E_ARG, std::string("write failed: ") + path);
 }
 
 void exfem_model_free(exfem_model *m) { delete m; }

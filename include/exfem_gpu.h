@@ -181,6 +181,17 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n);
  * *nsaved receives the number of stored samples per receiver. */
 int exfem_gpu_get_seismograms(exfem_ctx *ctx, double *out, size_t cap, int *nsaved);
 
+/* Displacement of right-hand side `rhs` at npoint arbitrary points for the
+ * current step, as visu_field (visualization.f90:156-181) samples the ANIMAT
+ * grid (visualize_solution, visualization.f90:192-284) from each step.bin:
+ * out[2*i], out[2*i+1] = (x, depth) at (xy[2*i], xy[2*i+1]) inside the
+ * 1-based element elem[i] (calcfieldat, formulation.f90:315-325), plus the
+ * free field at time steps_done * dt outside the DRM box.  elem[i] = 0 (no
+ * element holds the point) gives 0, as share_field fills unfound points
+ * (communicator.f90:1580-1584).  Waits for the context's queued steps;
+ * allocates device scratch for the points. */
+int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *xy, const int *elem, double *out);
+
 /* exfem_gpu_run() bracketed by CUDA events recorded on the context's own
  * stream; waits for completion and returns the device time in *ms.  A
  * measurement helper with no counterpart in the reference. */

@@ -67,6 +67,42 @@ int  exfem_write_step(const char *path, int append, int step, int ndofs,
 int  exfem_write_sheet(const char *path, int npoints, const double *points /* [2*npoints] */,
                        int nsave, const double *field, double samp);           /* io.cpp:844-889 */
 
+/* ANIMAT sampling grid (create_visualization, visualization.f90:24-54).
+ * visu_points (visualization.f90:129-154): nx = int((xmax-xmin)/dist),
+ * ny = int((ymax-ymin)/dist), points (xmin + i dist, ymin + j dist) with i
+ * outer and j inner.  Each point's element comes from a restatement of the
+ * reference's quadtree (order_quadtree/search_quadtree, quadtree.f90:21-251):
+ * ties on shared edges go to the larger coordinate, and points in no element
+ * (cut voids, outside the domain) get 0.  material holds visu_material's
+ * (material id, vp) at found points and 0 elsewhere (visualization.f90:
+ * 183-190, share_field's zero fill, communicator.f90:1580-1584).  The cells
+ * are create_struct_mesh's quads (mesh_utils.f90:846-878), 1-based. */
+typedef struct exfem_grid {
+    int    nx, ny;
+    double origin[2], space;
+    int    npoints;              /* (nx+1)*(ny+1)                                */
+    const double *points;        /* [2*npoints]                                   */
+    const int    *elem;          /* [npoints] 1-based element, 0 = not found      */
+    const double *material;      /* [2*npoints]                                   */
+    int    ncells;               /* nx*ny                                         */
+    const int    *eptr;          /* [ncells+1] 1-based                            */
+    const int    *eind;          /* [4*ncells] 1-based point ids                  */
+    int    nfound;
+} exfem_grid;
+
+int  exfem_model_grid(const exfem_model *m, double xmin, double xmax, double ymin, double ymax, double dist,
+                      exfem_grid **out);
+void exfem_grid_free(exfem_grid *g);
+
+/* VTK XML unstructured grid with base64 appended data, byte for byte the
+ * layout of write_vtk_unst_field (io.cpp:699-842): a 3-component Float32
+ * point array named fieldname (field is 2 values per point, the third 0),
+ * the points, connectivity/offsets/types of the cells.  io.cpp encodes the
+ * fourth byte of each block-length word from one byte past the int
+ * (io.cpp:657); this writer encodes the int's own fourth byte. */
+int  exfem_write_vtu(const char *path, int ncells, const int *eptr, const int *eind, int npoints,
+                     const double *points, const char *fieldname, const double *field);
+
 void exfem_model_free(exfem_model *m);
 
 #ifdef __cplusplus
