@@ -1107,7 +1107,9 @@ int f32_alloc(Ctx &c) {
     m.tcorn = nullptr;
     if (!c.use_tiles && !c.use_pipe) {
         std::vector<int> tc(4 * std::max<size_t>(P.tlist.size(), 1), 0);
-        for (size_t q = 0; q < P.tlist.size(); ++q) {
+        const long long nt = (long long)P.tlist.size();
+#pragma omp parallel for schedule(static)
+        for (long long q = 0; q < nt; ++q) {
             const int e = (P.tlist[q] >> 1) >> 2;
             for (int v = 0; v < 4; ++v) tc[4 * q + v] = P.econn[(size_t)e * 4 + v];
         }

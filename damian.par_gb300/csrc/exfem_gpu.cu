@@ -411,13 +411,7 @@ int create_device(Ctx &c, const exfem_mesh &mesh) {
     CK(cudaSetDevice(c.device));
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     // node coordinates in internal order (free field at DRM corners)
-    std::vector<double> nxy(2 * (size_t)c.plan.nn);
-    for (int i = 0; i < c.plan.nn; ++i) {
-        int rn = c.plan.ref_of_node[i];
-        nxy[2 * (size_t)i] = mesh.nodes[2 * (size_t)rn];
-        nxy[2 * (size_t)i + 1] = mesh.nodes[2 * (size_t)rn + 1];
-    }
-    TRY(upload(c, nxy, &c.dm.nxy));
+    TRY(upload(c, c.plan.nxy, &c.dm.nxy));   // internal node coordinates
     TRY(setup_device(c));
     c.block_threads = c.opts.block_threads > 0 ? c.opts.block_threads : 128;
     TRY(c.precision == EXFEM_FP64 ? alloc_fp64(c) : f32_alloc(c));

@@ -119,6 +119,56 @@ int init_wave_const(const exfem_wave &w, double alpha, double beta, WaveConst &o
     return EXFEM_OK;
 }
 
+// Stable LSD radix sort of the ids in idx by key[id]: 11-bit digits, so a
+// pass's 2048 scatter streams stay in cache; a pass whose digit is the same
+// for every key is skipped.  Each pass splits the array into fixed chunks that
+// count and scatter in parallel, with offsets laid out digit-major then
+// chunk-major, so the result is the stable order whatever the thread count.
+// Sorts contiguous (key, id) pairs so every pass streams through memory.
+static void radix_order(const std::vector<uint64_t> &key, std::vector<int> &idx) {
+    const long long n = (long long)idx.size();
+    if (n < 2) return;
+    constexpr int BITS = 11;
+    constexpr size_t NB = size_t(1) << BITS;
+    constexpr int NCH = 64;   // chunks per pass
+    const long long chunk = (n + NCH - 1) / NCH;
+    std::vector<std::pair<uint64_t, int>> a(n), b(n);
+    uint64_t any = 0, all = ~0ull;
+#pragma omp parallel for schedule(static) reduction(| : any) reduction(& : all)
+    for (long long i = 0; i < n; ++i) {
+        a[i] = {key[idx[i]], idx[i]};
+        any |= a[i].first;
+        all &= a[i].first;
+    }
+    std::vector<size_t> hist((size_t)NCH * NB);
+    for (int sh = 0; sh < 64; sh += BITS) {
+        if ((((any ^ all) >> sh) & (NB - 1)) == 0) continue;
+#pragma omp parallel for schedule(static, 1)
+        for (int t = 0; t < NCH; ++t) {
+            size_t *h = &hist[(size_t)t * NB];
+            std::fill(h, h + NB, 0);
+            const long long lo = t * chunk, hi = std::min(n, lo + chunk);
+            for (long long i = lo; i < hi; ++i) h[(a[i].first >> sh) & (NB - 1)]++;
+        }
+        size_t off = 0;
+        for (size_t d = 0; d < NB; ++d)
+            for (int t = 0; t < NCH; ++t) {
+                const size_t c = hist[(size_t)t * NB + d];
+                hist[(size_t)t * NB + d] = off;
+                off += c;
+            }
+#pragma omp parallel for schedule(static, 1)
+        for (int t = 0; t < NCH; ++t) {
+            size_t *h = &hist[(size_t)t * NB];
+            const long long lo = t * chunk, hi = std::min(n, lo + chunk);
+            for (long long i = lo; i < hi; ++i) b[h[(a[i].first >> sh) & (NB - 1)]++] = a[i];
+        }
+        a.swap(b);
+    }
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; ++i) idx[i] = a[i].second;
+}
+
 int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &P, std::string &err) {
     const int nn = mesh.nnodes, ne = mesh.nelems;
     if (nn <= 0 || ne <= 0 || !mesh.eptr || !mesh.eind || !mesh.ediv || !mesh.nodes || !mesh.ematprop) {
@@ -207,18 +257,19 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     // ---- internal numbering (Morton order; active nodes first, hanging last)
     std::vector<double> xs(nn), ys(nn);
     for (int i = 0; i < nn; ++i) { xs[i] = mesh.nodes[2 * i]; ys[i] = mesh.nodes[2 * i + 1]; }
-    std::vector<int> order(nn);
-    std::iota(order.begin(), order.end(), 0);
-    std::vector<uint64_t> keys(nn, 0);
+    // active nodes in Morton order (stable), then hanging entry i as node n_active + i
+    std::vector<int> order;
+    order.reserve(nn);
+    for (int i = 0; i < nn; ++i)
+        if (hang_of[i] < 0) order.push_back(i);
     Morton mort(xs, ys);
-    if (reorder)
+    if (reorder) {
+        std::vector<uint64_t> keys(nn, 0);
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < nn; ++i) keys[i] = mort.key(xs[i], ys[i]);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        bool ha = hang_of[a] >= 0, hb = hang_of[b] >= 0;
-        if (ha != hb) return !ha;
-        if (ha) return hang_of[a] < hang_of[b];   // hanging entry i -> internal n_active + i
-        return keys[a] < keys[b];
-    });
+        radix_order(keys, order);
+    }
+    for (int i = 0; i < prob.nhanging; ++i) order.push_back(prob.hanging[3 * i] - 1);
     P.ref_of_node = order;
     P.node_of_ref.assign(nn, -1);
     for (int i = 0; i < nn; ++i) P.node_of_ref[order[i]] = i;
@@ -229,19 +280,20 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     std::iota(eorder.begin(), eorder.end(), 0);
     if (reorder) {
         std::vector<uint64_t> ek(ne);
+#pragma omp parallel for schedule(static)
         for (int e = 0; e < ne; ++e) {
             const int *c = &corner_ref[(size_t)e * 4];
             double cx = 0.25 * (xs[c[0]] + xs[c[1]] + xs[c[2]] + xs[c[3]]);
             double cy = 0.25 * (ys[c[0]] + ys[c[1]] + ys[c[2]] + ys[c[3]]);
             ek[e] = mort.key(cx, cy);
         }
-        std::stable_sort(eorder.begin(), eorder.end(), [&](int a, int b) { return ek[a] < ek[b]; });
+        radix_order(ek, eorder);
     }
     P.ref_of_elem = eorder;
     std::vector<int> elem_of_ref(ne);
     for (int e = 0; e < ne; ++e) elem_of_ref[eorder[e]] = e;
 
-    // ---- per-element data (internal order)
+    // ---- per-element data (internal order); dashpot slots numbered in that order
     P.econn.resize((size_t)ne * 4);
     P.ecoef.resize((size_t)ne * 4);
     P.ecoef32.resize((size_t)ne * 4);
@@ -250,17 +302,17 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     P.edamp.assign(ne, -1);
     P.edampv.clear();
     std::vector<double> eh(ne);
+    std::vector<char> damped(ne, 0);
+    int bad_elem = ne;   // first element (reference id) with a bad length or density
+#pragma omp parallel for schedule(static) reduction(min : bad_elem)
     for (int ie = 0; ie < ne; ++ie) {
         int e = eorder[ie];
         const int *c = &corner_ref[(size_t)e * 4];
         for (int k = 0; k < 4; ++k) P.econn[(size_t)ie * 4 + k] = P.node_of_ref[c[k]];
         const double *mc = &prob.matconst[5 * (mesh.ematprop[e] - 1)];
-        double mu = mc[0], lam = mc[1], rho = mc[2], vp = mc[3], vs = mc[4];
+        double mu = mc[0], lam = mc[1], rho = mc[2];
         double h = ys[c[2]] - ys[c[0]];   // elength (model.f90:112-118)
-        if (!(h > 0) || !(rho > 0)) {
-            err = "element " + std::to_string(e + 1) + " has non-positive length or density";
-            return EXFEM_E_MESH;
-        }
+        if (!(h > 0) || !(rho > 0)) { bad_elem = std::min(bad_elem, e); continue; }
         eh[ie] = h;
         P.emulam[(size_t)ie * 2] = mu;
         P.emulam[(size_t)ie * 2 + 1] = lam;
@@ -271,34 +323,75 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         for (int k = 0; k < 4; ++k) P.ecoef32[(size_t)ie * 4 + k] = (float)P.ecoef[(size_t)ie * 4 + k];
         double scl = h / 2.0;
         P.emass[ie] = (scl * scl) * rho;   // calcm (formulation.f90:250-254)
-        double damping[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        bool any = false;
-        for (int k = 0; k < 4; ++k) {   // getdampingof + lysmer (model.f90:585-604)
+        for (int k = 0; k < 4; ++k) {
             int ab = prob.absorbing[c[k]];
-            if (ab == 1 || ab == 2) {
-                double r0 = vp * rho * h, r1 = vs * rho * h;
-                if (ab == 1) { damping[2 * k] = r1; damping[2 * k + 1] = r0; }
-                else { damping[2 * k] = r0; damping[2 * k + 1] = r1; }
-                any = true;
-            }
-        }
-        if (any) {
-            P.edamp[ie] = (int)(P.edampv.size() / 8);
-            P.edampv.insert(P.edampv.end(), damping, damping + 8);
+            if (ab == 1 || ab == 2) damped[ie] = 1;
         }
     }
-    // ---- m_full (init_explicit, explicit.f90:95-106) in reference order
-    P.mfull_ref.assign((size_t)2 * nn, 0.0);
-    for (int e = 0; e < ne; ++e) {
-        int ie = elem_of_ref[e];
-        const int *c = &corner_ref[(size_t)e * 4];
-        double mass = P.emass[ie];
-        const double *dv = P.edamp[ie] >= 0 ? &P.edampv[(size_t)P.edamp[ie] * 8] : nullptr;
-        for (int k = 0; k < 8; ++k) {
-            double damping = dv ? dv[k] : 0.0;
-            size_t d = (size_t)c[k / 2] * 2 + (k & 1);
-            P.mfull_ref[d] = P.mfull_ref[d] + (P.a2 * damping + P.a1 * mass);
+    if (bad_elem < ne) {
+        err = "element " + std::to_string(bad_elem + 1) + " has non-positive length or density";
+        return EXFEM_E_MESH;
+    }
+    {
+        int nd = 0;
+        for (int ie = 0; ie < ne; ++ie)
+            if (damped[ie]) P.edamp[ie] = nd++;
+        P.edampv.assign((size_t)nd * 8, 0.0);
+#pragma omp parallel for schedule(static)
+        for (int ie = 0; ie < ne; ++ie) {
+            if (!damped[ie]) continue;
+            int e = eorder[ie];
+            const int *c = &corner_ref[(size_t)e * 4];
+            const double *mc = &prob.matconst[5 * (mesh.ematprop[e] - 1)];
+            const double rho = mc[2], vp = mc[3], vs = mc[4], h = eh[ie];
+            double *damping = &P.edampv[(size_t)P.edamp[ie] * 8];
+            for (int k = 0; k < 4; ++k) {   // getdampingof + lysmer (model.f90:585-604)
+                int ab = prob.absorbing[c[k]];
+                if (ab == 1 || ab == 2) {
+                    double r0 = vp * rho * h, r1 = vs * rho * h;
+                    if (ab == 1) { damping[2 * k] = r1; damping[2 * k + 1] = r0; }
+                    else { damping[2 * k] = r0; damping[2 * k + 1] = r1; }
+                }
+            }
         }
+    }
+    // ---- own incidences per node (internal ids), reference element order
+    P.ownptr.assign(nn + 1, 0);
+    for (int ie = 0; ie < ne; ++ie)
+        for (int k = 0; k < 4; ++k) P.ownptr[P.econn[(size_t)ie * 4 + k] + 1]++;
+    for (int i = 0; i < nn; ++i) P.ownptr[i + 1] += P.ownptr[i];
+    P.ownlist.resize(P.ownptr[nn]);
+    {
+        std::vector<int> fill(P.ownptr.begin(), P.ownptr.end() - 1);
+        for (int e = 0; e < ne; ++e) {   // reference element order
+            int ie = elem_of_ref[e];
+            for (int k = 0; k < 4; ++k) P.ownlist[fill[P.econn[(size_t)ie * 4 + k]]++] = ie * 4 + k;
+        }
+    }
+    for (int i = 0; i < nn; ++i)
+        if (P.ownptr[i + 1] == P.ownptr[i]) {
+            err = "node " + std::to_string(P.ref_of_node[i] + 1) + " is not a non-hanging corner of any element";
+            return EXFEM_E_MESH;
+        }
+    // ---- m_full (init_explicit, explicit.f90:95-106): each dof sums its
+    // element terms in reference element order (the incidence lists' order),
+    // as the element loop adds them; then sum_reactanchors in halving form
+    P.mfull_ref.assign((size_t)2 * nn, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n < nn; ++n) {
+        const size_t x = (size_t)P.ref_of_node[n];
+        double acc[2] = {0.0, 0.0};
+        for (int q = P.ownptr[n]; q < P.ownptr[n + 1]; ++q) {
+            const int ie = P.ownlist[q] >> 2, k = P.ownlist[q] & 3;
+            const double mass = P.emass[ie];
+            const double *dv = P.edamp[ie] >= 0 ? &P.edampv[(size_t)P.edamp[ie] * 8] : nullptr;
+            for (int d = 0; d < 2; ++d) {
+                double damping = dv ? dv[2 * k + d] : 0.0;
+                acc[d] = acc[d] + (P.a2 * damping + P.a1 * mass);
+            }
+        }
+        P.mfull_ref[2 * x] = acc[0];
+        P.mfull_ref[2 * x + 1] = acc[1];
     }
     for (int i = 0; i < prob.nhanging; ++i) {   // sum_reactanchors, halving form
         int h = prob.hanging[3 * i] - 1, a = prob.hanging[3 * i + 1] - 1, b = prob.hanging[3 * i + 2] - 1;
@@ -317,66 +410,73 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             P.inv_mfull[(size_t)2 * n + k] = 1.0 / m;
             P.mfull_int[(size_t)2 * n + k] = m;
         }
-    // ---- own incidences per node (internal ids), element order
-    P.ownptr.assign(nn + 1, 0);
-    for (int ie = 0; ie < ne; ++ie)
-        for (int k = 0; k < 4; ++k) P.ownptr[P.econn[(size_t)ie * 4 + k] + 1]++;
-    for (int i = 0; i < nn; ++i) P.ownptr[i + 1] += P.ownptr[i];
-    P.ownlist.resize(P.ownptr[nn]);
-    {
-        std::vector<int> fill(P.ownptr.begin(), P.ownptr.end() - 1);
-        for (int e = 0; e < ne; ++e) {   // reference element order
-            int ie = elem_of_ref[e];
-            for (int k = 0; k < 4; ++k) P.ownlist[fill[P.econn[(size_t)ie * 4 + k]]++] = ie * 4 + k;
-        }
-    }
-    for (int i = 0; i < nn; ++i)
-        if (P.ownptr[i + 1] == P.ownptr[i]) {
-            err = "node " + std::to_string(P.ref_of_node[i] + 1) + " is not a non-hanging corner of any element";
-            return EXFEM_E_MESH;
-        }
-    // ---- hanging entries (internal) and per-anchor links
+    // ---- hanging entries (internal) and per-anchor links (h, other anchor), entry order
     P.hang.resize((size_t)3 * P.n_hang);
-    std::vector<std::vector<std::pair<int, int>>> links(P.n_active);   // anchor -> (h, other anchor)
+    P.lptr.assign(P.n_active + 1, 0);
     for (int i = 0; i < prob.nhanging; ++i) {
         int h = P.node_of_ref[prob.hanging[3 * i] - 1];
         int a = P.node_of_ref[prob.hanging[3 * i + 1] - 1];
         int b = P.node_of_ref[prob.hanging[3 * i + 2] - 1];
         P.hang[3 * (size_t)i] = h; P.hang[3 * (size_t)i + 1] = a; P.hang[3 * (size_t)i + 2] = b;
-        links[a].push_back({h, b});
-        links[b].push_back({h, a});
+        P.lptr[a + 1]++;
+        P.lptr[b + 1]++;
     }
-    P.lptr.assign(P.n_active + 1, 0);
-    P.llist.clear();
-    for (int n = 0; n < P.n_active; ++n) {
-        for (auto &pr : links[n]) { P.llist.push_back(pr.first); P.llist.push_back(pr.second); }
-        P.lptr[n + 1] = (int)(P.llist.size() / 2);
+    for (int n = 0; n < P.n_active; ++n) P.lptr[n + 1] += P.lptr[n];
+    P.llist.assign(2 * (size_t)P.lptr[P.n_active], 0);
+    {
+        std::vector<int> fill(P.lptr.begin(), P.lptr.end() - 1);
+        for (int i = 0; i < prob.nhanging; ++i) {
+            int h = P.hang[3 * (size_t)i], a = P.hang[3 * (size_t)i + 1], b = P.hang[3 * (size_t)i + 2];
+            int qa = fill[a]++, qb = fill[b]++;
+            P.llist[2 * (size_t)qa] = h; P.llist[2 * (size_t)qa + 1] = b;
+            P.llist[2 * (size_t)qb] = h; P.llist[2 * (size_t)qb + 1] = a;
+        }
     }
     // ---- gather lists of active nodes: own terms, then linked hanging terms at 1/2
     P.tptr.assign(P.n_active + 1, 0);
-    P.tlist.clear();
-    P.tlist.reserve(P.ownlist.size() + 8 * P.n_hang);
+#pragma omp parallel for schedule(static)
     for (int n = 0; n < P.n_active; ++n) {
-        for (int q = P.ownptr[n]; q < P.ownptr[n + 1]; ++q) P.tlist.push_back(P.ownlist[q] << 1);
-        for (auto &pr : links[n])
-            for (int q = P.ownptr[pr.first]; q < P.ownptr[pr.first + 1]; ++q) P.tlist.push_back((P.ownlist[q] << 1) | 1);
-        P.tptr[n + 1] = (int)P.tlist.size();
+        int cnt = P.ownptr[n + 1] - P.ownptr[n];
+        for (int q = P.lptr[n]; q < P.lptr[n + 1]; ++q) {
+            int h = P.llist[2 * (size_t)q];
+            cnt += P.ownptr[h + 1] - P.ownptr[h];
+        }
+        P.tptr[n + 1] = cnt;
+    }
+    for (int n = 0; n < P.n_active; ++n) P.tptr[n + 1] += P.tptr[n];
+    P.tlist.assign(P.tptr[P.n_active], 0);
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n < P.n_active; ++n) {
+        int o = P.tptr[n];
+        for (int q = P.ownptr[n]; q < P.ownptr[n + 1]; ++q) P.tlist[o++] = P.ownlist[q] << 1;
+        for (int l = P.lptr[n]; l < P.lptr[n + 1]; ++l) {
+            int h = P.llist[2 * (size_t)l];
+            for (int q = P.ownptr[h]; q < P.ownptr[h + 1]; ++q) P.tlist[o++] = (P.ownlist[q] << 1) | 1;
+        }
     }
     // ---- per-node lumped mass / damping (internal), for the FP32 increment form
     P.nmass.assign(nn, 0.0);
     P.ndamp.assign((size_t)2 * nn, 0.0);
-    for (int ie = 0; ie < ne; ++ie) {
-        const double *dv = P.edamp[ie] >= 0 ? &P.edampv[(size_t)P.edamp[ie] * 8] : nullptr;
-        for (int k = 0; k < 4; ++k) {
-            int x = P.econn[(size_t)ie * 4 + k];
-            P.nmass[x] += P.emass[ie];
-            if (dv) { P.ndamp[2 * (size_t)x] += dv[2 * k]; P.ndamp[2 * (size_t)x + 1] += dv[2 * k + 1]; }
+#pragma omp parallel for schedule(static)
+    for (int x = 0; x < nn; ++x) {
+        double ms = 0.0, d0 = 0.0, d1 = 0.0;
+        for (int q = P.ownptr[x]; q < P.ownptr[x + 1]; ++q) {
+            const int ie = P.ownlist[q] >> 2, k = P.ownlist[q] & 3;
+            ms += P.emass[ie];
+            if (P.edamp[ie] >= 0) {
+                const double *dv = &P.edampv[(size_t)P.edamp[ie] * 8];
+                d0 += dv[2 * k];
+                d1 += dv[2 * k + 1];
+            }
         }
+        P.nmass[x] = ms;
+        P.ndamp[2 * (size_t)x] = d0;
+        P.ndamp[2 * (size_t)x + 1] = d1;
     }
     // ---- DRM slots (wave_elems output, model.f90:1015-1045)
     P.s_elem.resize(prob.nseismic);
     P.s_kind.resize(prob.nseismic);
-    std::vector<std::vector<int>> dl(P.n_active);
+    std::vector<std::pair<int, int>> dent;   // (active node, entry) in slot order
     for (int s = 0; s < prob.nseismic; ++s) {
         int e = prob.seismic[2 * s] - 1, kind = prob.seismic[2 * s + 1];
         if (e < 0 || e >= ne || !(kind == 1 || kind == 2 || kind == 4 || kind == 5 || kind == 6)) {
@@ -389,11 +489,11 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         for (int k = 0; k < 4; ++k) {
             int x = P.econn[(size_t)ie * 4 + k];
             int ent = (s * 4 + k) << 1;
-            if (x < P.n_active) dl[x].push_back(ent);
+            if (x < P.n_active) dent.push_back({x, ent});
             else {
                 int hi = hang_of[P.ref_of_node[x]];
-                dl[P.node_of_ref[prob.hanging[3 * hi + 1] - 1]].push_back(ent | 1);
-                dl[P.node_of_ref[prob.hanging[3 * hi + 2] - 1]].push_back(ent | 1);
+                dent.push_back({P.node_of_ref[prob.hanging[3 * hi + 1] - 1], ent | 1});
+                dent.push_back({P.node_of_ref[prob.hanging[3 * hi + 2] - 1], ent | 1});
             }
         }
     }
@@ -408,14 +508,17 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             for (int k = 0; k < 4; ++k) P.odlist[fill[P.econn[(size_t)P.s_elem[s] * 4 + k]]++] = s * 4 + k;
     }
     P.dptr.assign(P.n_active + 1, 0);
-    P.dlist.clear();
-    for (int n = 0; n < P.n_active; ++n) {
-        P.dlist.insert(P.dlist.end(), dl[n].begin(), dl[n].end());
-        P.dptr[n + 1] = (int)P.dlist.size();
+    for (auto &de : dent) P.dptr[de.first + 1]++;
+    for (int n = 0; n < P.n_active; ++n) P.dptr[n + 1] += P.dptr[n];
+    P.dlist.assign(P.dptr[P.n_active], 0);
+    {
+        std::vector<int> fill(P.dptr.begin(), P.dptr.end() - 1);
+        for (auto &de : dent) P.dlist[fill[de.first]++] = de.second;
     }
     // ---- kept for point sampling
     P.elem_of_ref = elem_of_ref;
     P.nxy.resize(2 * (size_t)nn);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nn; ++i) {
         P.nxy[2 * (size_t)P.node_of_ref[i]] = xs[i];
         P.nxy[2 * (size_t)P.node_of_ref[i] + 1] = ys[i];

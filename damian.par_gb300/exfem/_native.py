@@ -84,7 +84,7 @@ def build_gpu(force=False):
         obj = os.path.join(BUILD, f + ".o")
         # host code never contracts a*b+c (g++ does on aarch64 by default),
         # so host-side FP64 setup rounds like the CPU oracle on both machines
-        host = ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+        host = ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp"]
         if f.endswith(".cu"):
             # *_nofma.cu keep the reference's separate roundings on the device
             fmad = ["-fmad=false"] if f.endswith("_nofma.cu") else []
@@ -99,7 +99,7 @@ def build_gpu(force=False):
     with ThreadPoolExecutor(max_workers=min(8, max(1, len(units)))) as ex:
         objs = list(ex.map(compile_unit, units))
     tmp = GPU_LIB + ".tmp%d" % os.getpid()
-    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lgomp"])
     os.replace(tmp, GPU_LIB)
     return GPU_LIB
 
