@@ -1,6 +1,7 @@
 // exfem_srv.cpp — continuous-batching server over the exfem_gpu C ABI
 // (include/exfem_srv.h).  Host code only: every device action goes through
 // exfem_gpu_* on the request's own context and stream.
+#include "exfem_host.h"
 #include "exfem_srv.h"
 
 #include <cuda_runtime.h>
@@ -19,7 +20,7 @@
 
 namespace {
 
-enum State { WAITING, PREPARING, ACTIVE, DONE };
+enum State { MESHING, WAITING, PREPARING, ACTIVE, DONE };
 
 struct Req {
     long long id = 0;
@@ -34,12 +35,17 @@ struct Req {
     std::vector<exfem_wave> waves;
     exfem_mesh mesh{};
     exfem_problem prob{};
+    std::string deck;                  // deck requests: the text, then the model built from it
+    exfem_model *model = nullptr;
     size_t est = 0, held = 0, actual = 0;
     exfem_ctx *ctx = nullptr;
     int bypassed = 0;
-    double t_submit = 0, t_admit = 0, t_ready = 0, t_done = 0;
+    double t_submit = 0, t_meshed = 0, t_admit = 0, t_ready = 0, t_done = 0;
     std::vector<double> seis;
     bool reported = false;
+    ~Req() {
+        if (model) exfem_model_free(model);
+    }
 };
 
 template <typename T>
@@ -56,6 +62,8 @@ struct exfem_srv {
     std::map<long long, Req *> reqs;
     std::deque<Req *> waiting;
     std::deque<Req *> prep_queue;
+    std::deque<Req *> mesh_queue;   // deck requests to mesh
+    int meshing = 0;
     std::vector<Req *> active;
     std::deque<Req *> finished;
     size_t budget = 0, held = 0;
@@ -119,15 +127,60 @@ struct exfem_srv {
         cv_done.notify_all();
     }
 
+    // Builds a deck request's model (no lock held), then queues it for
+    // admission or finishes it with the deck's error.
+    void mesh_one(Req *r) {
+        exfem_model *m = nullptr;
+        int rc = exfem_model_build(r->deck.c_str(), &m);
+        if (!rc && r->nsteps > 0) rc = exfem_model_set_nsteps(m, r->nsteps);
+        std::string msg = rc ? exfem_model_error() : std::string();
+        size_t est = 0;
+        if (!rc) {
+            exfem_model_views(m, &r->mesh, &r->prob);
+            r->nsteps = r->prob.nsteps;
+            est = exfem_gpu_estimate_bytes(&r->mesh, &r->prob, &opts.solver);
+        } else if (m) {
+            exfem_model_free(m);
+            m = nullptr;
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        meshing--;
+        r->model = m;
+        r->deck.clear();
+        r->deck.shrink_to_fit();
+        r->t_meshed = now();
+        if (rc) {
+            r->err = msg;
+            r->t_admit = r->t_ready = r->t_meshed;
+            finish(r, rc);
+        } else {
+            r->est = est;
+            r->state = WAITING;
+            waiting.push_back(r);
+        }
+        cv_sched.notify_one();
+    }
+
     void prep_loop() {
         for (;;) {
             Req *r = nullptr;
+            bool mesh_job = false;
             {
                 std::unique_lock<std::mutex> lk(mu);
-                cv_prep.wait(lk, [&] { return stop || !prep_queue.empty(); });
-                if (stop && prep_queue.empty()) return;
-                r = prep_queue.front();
-                prep_queue.pop_front();
+                cv_prep.wait(lk, [&] { return stop || !prep_queue.empty() || !mesh_queue.empty(); });
+                if (stop && prep_queue.empty()) return;   // queued decks are dropped on close
+                if (!prep_queue.empty()) {   // admitted requests first: they feed the GPU
+                    r = prep_queue.front();
+                    prep_queue.pop_front();
+                } else {
+                    r = mesh_queue.front();
+                    mesh_queue.pop_front();
+                    mesh_job = true;
+                }
+            }
+            if (mesh_job) {
+                mesh_one(r);
+                continue;
             }
             exfem_ctx *ctx = nullptr;
             int rc = exfem_gpu_create(&r->mesh, &r->prob, &opts.solver, &ctx);
@@ -302,11 +355,34 @@ int exfem_srv_submit(exfem_srv *s, const exfem_mesh *mesh, const exfem_problem *
     r->est = exfem_gpu_estimate_bytes(&r->mesh, &r->prob, &s->opts.solver);
     std::lock_guard<std::mutex> lk(s->mu);
     r->id = s->next_id++;
-    r->t_submit = s->now();
+    r->t_submit = r->t_meshed = s->now();
     s->reqs[r->id] = r;
     s->waiting.push_back(r);
     if (id) *id = r->id;
     s->cv_sched.notify_one();
+    return EXFEM_OK;
+}
+
+int exfem_srv_submit_deck(exfem_srv *s, const char *deck, int nsteps, long long *id) {
+    if (!s || !deck) return EXFEM_E_ARG;
+    Req *r = new (std::nothrow) Req();
+    if (!r) return EXFEM_E_NOMEM;
+    try {
+        r->deck = deck;
+    } catch (...) {
+        delete r;
+        return EXFEM_E_NOMEM;
+    }
+    r->nsteps = nsteps > 0 ? nsteps : 0;
+    r->state = MESHING;
+    std::lock_guard<std::mutex> lk(s->mu);
+    r->id = s->next_id++;
+    r->t_submit = s->now();
+    s->reqs[r->id] = r;
+    s->mesh_queue.push_back(r);
+    s->meshing++;
+    if (id) *id = r->id;
+    s->cv_prep.notify_one();
     return EXFEM_OK;
 }
 
@@ -331,6 +407,7 @@ int exfem_srv_poll(exfem_srv *s, exfem_srv_result *out, int cap, int wait_ms) {
         o.device_bytes = r->actual;
         o.reserved_bytes = r->est;
         o.t_submit = r->t_submit;
+        o.t_meshed = r->t_meshed;
         o.t_admit = r->t_admit;
         o.t_ready = r->t_ready;
         o.t_done = r->t_done;
@@ -359,7 +436,7 @@ int exfem_srv_stats(exfem_srv *s, int *waiting, int *preparing, int *active, lon
                     int *peak_active) {
     if (!s) return EXFEM_E_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
-    if (waiting) *waiting = (int)s->waiting.size();
+    if (waiting) *waiting = (int)s->waiting.size() + s->meshing;   // deck requests still meshing count as waiting
     if (preparing) *preparing = s->preparing;
     if (active) *active = (int)s->active.size();
     if (finished) *finished = s->n_finished;

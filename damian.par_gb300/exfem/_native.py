@@ -57,7 +57,7 @@ def host_sources():
 def gpu_sources():
     srcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
                   if f.endswith((".cu", ".cpp", ".cuh", ".h")))
-    return srcs + sorted(os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h"))
+    return srcs + sorted(os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")) + [HOST_LIB]
 
 
 def build_host(force=False):
@@ -72,7 +72,9 @@ def build_host(force=False):
 
 
 def build_gpu(force=False):
-    """Compile every .cu/.cpp of csrc/ for sm_103a in parallel and link the .so."""
+    """Compile every .cu/.cpp of csrc/ for sm_103a in parallel and link the .so
+    (against the host library, which it needs for the server's decks)."""
+    build_host(force)
     os.makedirs(BUILD, exist_ok=True)
     if not force and _newer(GPU_LIB, gpu_sources()):
         return GPU_LIB
@@ -99,7 +101,9 @@ def build_gpu(force=False):
     with ThreadPoolExecutor(max_workers=min(8, max(1, len(units)))) as ex:
         objs = list(ex.map(compile_unit, units))
     tmp = GPU_LIB + ".tmp%d" % os.getpid()
-    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lgomp"])
+    # the server meshes decks with the host library, found beside this one
+    _run([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-L", BUILD, "-lexfem_host", "-Xlinker", "-rpath",
+          "-Xlinker", "$ORIGIN", "-lcudart", "-lgomp"])
     os.replace(tmp, GPU_LIB)
     return GPU_LIB
 

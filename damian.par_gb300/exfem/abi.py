@@ -96,7 +96,7 @@ class SrvResult(C.Structure):
                 ("nrhs", C.c_int), ("nrecv", C.c_int), ("nsave", C.c_int), ("device_bytes", C.c_size_t),
                 ("reserved_bytes", C.c_size_t),
                 ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_ready", C.c_double),
-                ("t_done", C.c_double)]
+                ("t_done", C.c_double), ("t_meshed", C.c_double)]
 
 
 SRV_SYMBOLS = {
@@ -104,6 +104,7 @@ SRV_SYMBOLS = {
     "exfem_srv_open": (C.c_int, [C.POINTER(SrvOpts), C.POINTER(C.c_void_p)]),
     "exfem_srv_submit": (C.c_int, [C.c_void_p, C.POINTER(Mesh), C.POINTER(Problem), C.c_int,
                                    C.POINTER(C.c_longlong)]),
+    "exfem_srv_submit_deck": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.POINTER(C.c_longlong)]),
     "exfem_srv_poll": (C.c_int, [C.c_void_p, C.POINTER(SrvResult), C.c_int, C.c_int]),
     "exfem_srv_fetch": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_double), C.c_size_t]),
     "exfem_srv_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),

@@ -60,6 +60,14 @@ class Server:
         self.models[rid.value] = model
         return rid.value
 
+    def submit_deck(self, deck, nsteps=None):
+        """Queue problem.in text; the server meshes it on a worker thread."""
+        rid = C.c_longlong()
+        rc = self.L.exfem_srv_submit_deck(self.h, deck.encode(), 0 if nsteps is None else int(nsteps), C.byref(rid))
+        if rc != 0:
+            raise ExfemError(rc, self.L.exfem_srv_last_error(self.h).decode())
+        return rid.value
+
     def poll(self, wait_ms=0, cap=64):
         buf = (SrvResult * cap)()
         n = self.L.exfem_srv_poll(self.h, buf, cap, int(wait_ms))
@@ -114,8 +122,9 @@ class Server:
 
 
 def run_stream(requests, server_kw=None, keep_seis=False, timeout=3600.0):
-    """Replay [(arrival_s, model, nsteps), ...] in real time against a new
-    server.  Returns per-request records and a summary (p50/p99 latency,
+    """Replay [(arrival_s, model or deck text, nsteps), ...] in real time
+    against a new server (deck text is meshed by the server, inside the
+    latency).  Returns per-request records and a summary (p50/p99 latency,
     throughput in elem-steps*rhs/s over the makespan)."""
     server_kw = server_kw or {}
     recs = {}
@@ -129,9 +138,11 @@ def run_stream(requests, server_kw=None, keep_seis=False, timeout=3600.0):
             now = time.perf_counter() - t0
             while i < len(pending) and pending[i][0] <= now:
                 arr, model, nsteps = pending[i]
-                rid = srv.submit(model, nsteps)
-                recs[rid] = {"arrival": arr, "submitted": time.perf_counter() - t0, "nelems": model.nelems,
-                             "nrhs": model.problem.nrhs, "nsteps": nsteps}
+                if isinstance(model, str):
+                    rid = srv.submit_deck(model, nsteps)
+                else:
+                    rid = srv.submit(model, nsteps)
+                recs[rid] = {"arrival": arr, "submitted": time.perf_counter() - t0, "nsteps": nsteps}
                 i += 1
             wait = 0 if i < len(pending) else 50
             if i < len(pending):
@@ -141,6 +152,8 @@ def run_stream(requests, server_kw=None, keep_seis=False, timeout=3600.0):
                 r["finished"] = time.perf_counter() - t0
                 r["status"] = d["status"]
                 r["t_admit"], r["t_ready"], r["t_done"] = d["t_admit"], d["t_ready"], d["t_done"]
+                r["t_meshed"], r["t_submit"] = d["t_meshed"], d["t_submit"]   # server clock
+                r["nelems"], r["nrhs"], r["nsteps"] = d["nelems"], d["nrhs"], d["nsteps"]
                 r["latency"] = r["finished"] - r["arrival"]
                 if d["status"] == 0:
                     s = srv.fetch(d["id"])

@@ -11,6 +11,9 @@
  *     a larger one at the head, which is protected from starving;
  *   - device setup of admitted requests (exfem_gpu_create, init_explicit)
  *     runs on preparer threads so it never stalls the stepping;
+ *   - requests may arrive as problem.in text: the same threads run the host
+ *     mesher (include/exfem_host.h) before admission, so meshing overlaps
+ *     the stepping of other requests;
  *   - the scheduler thread advances every running request by chunks of steps
  *     and collects the seismograms of finished ones, freeing their memory.
  * Each request computes exactly what exfem_gpu_run would compute for it
@@ -44,6 +47,7 @@ typedef struct exfem_srv_result {
     size_t    device_bytes;    /* bytes its context held                        */
     size_t    reserved_bytes;  /* footprint reserved at admission (upper bound)  */
     double    t_submit, t_admit, t_ready, t_done;
+    double    t_meshed;        /* mesh built (deck requests; = t_submit otherwise) */
 } exfem_srv_result;
 
 void exfem_srv_default_opts(exfem_srv_opts *opts);
@@ -54,6 +58,13 @@ int  exfem_srv_open(const exfem_srv_opts *opts, exfem_srv **out);
 int  exfem_srv_submit(exfem_srv *srv, const exfem_mesh *mesh, const exfem_problem *prob, int nsteps,
                       long long *id);
 
+/* Queue one problem given as problem.in text (the deck format of
+ * include/exfem_host.h).  A preparer thread builds its mesh and problem as
+ * the Fortran host's init_model would (explicit.f90:16-70), then it waits
+ * for admission like any other request.  nsteps <= 0 runs the deck's own
+ * step count.  Deck errors come back as the request's status. */
+int  exfem_srv_submit_deck(exfem_srv *srv, const char *deck, int nsteps, long long *id);
+
 /* Finished requests not reported before (up to cap), waiting up to wait_ms
  * for at least one.  Returns how many were written. */
 int  exfem_srv_poll(exfem_srv *srv, exfem_srv_result *out, int cap, int wait_ms);
@@ -62,7 +73,8 @@ int  exfem_srv_poll(exfem_srv *srv, exfem_srv_result *out, int cap, int wait_ms)
  * exfem_gpu_get_seismograms; releases the request's host copy. */
 int  exfem_srv_fetch(exfem_srv *srv, long long id, double *out, size_t cap);
 
-/* Counters: requests waiting, being prepared, stepping, finished; bytes held. */
+/* Counters: requests waiting (deck requests still meshing included), being
+ * prepared, stepping, finished; bytes held. */
 int  exfem_srv_stats(exfem_srv *srv, int *waiting, int *preparing, int *active, long long *finished,
                      size_t *bytes_held, int *peak_active);
 

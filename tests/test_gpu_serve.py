@@ -94,3 +94,36 @@ def test_timed_stream_reports_latency_and_throughput():
     recs, summary, _ = run_stream(reqs, server_kw={"max_active": 6, "chunk_steps": 64})
     assert summary["ok"] == 10 and 0 < summary["p50_s"] <= summary["p99_s"]
     assert summary["throughput"] > 0
+
+
+def test_deck_requests_match_model_requests():
+    """Requests given as problem.in text are meshed by the server's worker
+    threads before admission and give the same seismograms as the same
+    problems built on the caller's side; a bad deck fails alone."""
+    stream = decks.serving_stream(n=4, seed=5, min_scale=0.08, max_scale=0.15, max_angles=3, step_range=(100, 300))
+    with Server(max_active=4, chunk_steps=64) as srv:
+        ids_deck = [srv.submit_deck(d, n) for _, d, n in stream]
+        bad = srv.submit_deck("PROBLEM FILE EXFEM\nDOMAIN:\n-1 -1\n", 10)
+        models = [Model(d, nsteps=n) for _, d, n in stream]
+        ids_model = [srv.submit(m, n) for m, (_, _, n) in zip(models, stream)]
+        res = {r["id"]: r for r in srv.wait_all(2 * len(stream) + 1)}
+        assert res[bad]["status"] != 0
+        for i in ids_deck:
+            r = res[i]
+            assert r["status"] == 0
+            assert r["t_submit"] <= r["t_meshed"] <= r["t_admit"] <= r["t_ready"] <= r["t_done"]
+        got_deck = [srv.fetch(i) for i in ids_deck]
+        got_model = [srv.fetch(i) for i in ids_model]
+        with pytest.raises(Exception):
+            srv.fetch(bad)
+    for a, b, (_, _, n) in zip(got_deck, got_model, stream):
+        assert a.shape == b.shape and np.array_equal(a, b)
+
+
+def test_stream_of_decks_reports_latency_with_meshing():
+    stream = decks.serving_stream(n=6, rate=40.0, seed=3, min_scale=0.08, max_scale=0.2, max_angles=4,
+                                  step_range=(100, 400))
+    recs, summary, _ = run_stream(stream, server_kw={"max_active": 4, "chunk_steps": 64})
+    assert summary["ok"] == len(stream)
+    for r in recs.values():
+        assert r["t_meshed"] >= r["t_submit"] and r["latency"] > 0 and r["nelems"] > 0
