@@ -28,7 +28,6 @@
 #include <random>
 #include <sstream>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 namespace {
@@ -600,6 +599,13 @@ inline uint64_t pairkey(int a, int b) {
 // selection of mesh_utils.f90:114-201 and the construction of
 // mesh_utils.f90:203-409, 454-681, all on a single rank.
 bool Model::divide_pass() {
+    // One pass of the reference's division (select_local_divide, create_*nodes,
+    // select_newhanging, final_division; mesh_utils.f90:114-681).  New nodes are
+    // numbered in the reference's order: edge nodes of divided elements with a
+    // larger neighbour, then those under an undivided smaller neighbour, then
+    // centres, then edges without a neighbour, each in element order.  Every
+    // phase counts per element, takes a prefix sum and fills in parallel, so
+    // the numbering is the sequential one.
     const int n = ne();
     const int nn = (int)nx.size();
     // node -> element incidence over full CSR (hanging slots included)
@@ -612,38 +618,56 @@ bool Model::divide_pass() {
         for (int e = 0; e < n; ++e)
             for (int j = eptr[e]; j < eptr[e + 1]; ++j) nel[fill[eind[j]]++] = e;
     }
-    // dual graph with ncommon = 2 (parmetis_v3_mesh2dual, communicator.f90:496-514)
-    std::vector<int> aptr(n + 1, 0), adj;
-    adj.reserve((size_t)n * 4);
-    {
-        std::vector<int> cnt(n, 0), touched;
-        for (int e = 0; e < n; ++e) {
-            touched.clear();
-            for (int j = eptr[e]; j < eptr[e + 1]; ++j) {
-                int v = eind[j];
-                for (int q = nptr[v]; q < nptr[v + 1]; ++q) {
-                    int f = nel[q];
-                    if (f == e) continue;
-                    if (cnt[f] == 0) touched.push_back(f);
-                    cnt[f]++;
-                }
-            }
-            std::sort(touched.begin(), touched.end());
-            for (int f : touched) { if (cnt[f] >= 2) adj.push_back(f); cnt[f] = 0; }
-            aptr[e + 1] = (int)adj.size();
+    // dual graph with ncommon = 2 (parmetis_v3_mesh2dual, communicator.f90:496-514),
+    // each element's neighbours in ascending order
+    constexpr int MAXN = 16;
+    std::vector<int> nbuf((size_t)n * MAXN), deg(n, 0);
+    int overflow = 0;
+#pragma omp parallel for schedule(static) reduction(| : overflow)
+    for (int e = 0; e < n; ++e) {
+        int cand[128];
+        int nc = 0;
+        for (int j = eptr[e]; j < eptr[e + 1]; ++j) {
+            const int v = eind[j];
+            for (int q = nptr[v]; q < nptr[v + 1]; ++q)
+                if (nel[q] != e && nc < 128) cand[nc++] = nel[q];
         }
+        std::sort(cand, cand + nc);
+        int d = 0;
+        for (int i = 0; i < nc;) {
+            int k = i + 1;
+            while (k < nc && cand[k] == cand[i]) ++k;
+            if (k - i >= 2) {
+                if (d < MAXN) nbuf[(size_t)e * MAXN + d] = cand[i];
+                ++d;
+            }
+            i = k;
+        }
+        if (d > MAXN || nc >= 128) overflow = 1;
+        deg[e] = std::min(d, MAXN);
     }
+    if (overflow) {   // cannot happen on a 2:1 quadtree; keep the mesh as it is
+        return false;
+    }
+    std::vector<int> aptr(n + 1, 0);
+    for (int e = 0; e < n; ++e) aptr[e + 1] = aptr[e] + deg[e];
+    std::vector<int> adj(aptr[n]);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < n; ++e)
+        for (int d = 0; d < deg[e]; ++d) adj[aptr[e] + d] = nbuf[(size_t)e * MAXN + d];
+    std::vector<int>().swap(nbuf);
     auto hanging_element = [&](int e) { return (eptr[e + 1] - eptr[e]) > 4; };   // model.f90:454-458
     // select_local_divide (mesh_utils.f90:114-154)
     std::vector<uint8_t> todiv(n, 0);
-    bool further = false;
+    int further = 0;
+#pragma omp parallel for schedule(static) reduction(| : further)
     for (int e = 0; e < n; ++e) {
         if (needs_division(e) && !hanging_element(e)) {
             bool ok = true;
             for (int q = aptr[e]; q < aptr[e + 1]; ++q)
                 if (hanging_element(adj[q])) { ok = false; break; }
             todiv[e] = ok;
-            further = further || ok;
+            further |= ok ? 1 : 0;
         }
     }
     if (!further) return false;
@@ -666,130 +690,213 @@ bool Model::divide_pass() {
         px = (nx[a] + nx[b]) / 2.0;
         py = (ny[a] + ny[b]) / 2.0;
     };
-    std::unordered_map<uint64_t, int> edgenode;
-    edgenode.reserve((size_t)n);
-    std::vector<double> addx, addy;
+    // the slot of i in k's neighbour list
+    auto slot_of = [&](int k, int i) -> int {
+        for (int q = aptr[k]; q < aptr[k + 1]; ++q)
+            if (adj[q] == i) return q;
+        return -1;
+    };
+    // adjnode[q]: the node created on the edge between element e and adj[q]
+    // (both slots of the pair carry it), -1 if none
+    std::vector<int> adjnode(aptr[n], -1);
+    std::vector<int> cnt(n + 1, 0);
     const int base = nn;
+    int next = base;
+    auto scan = [&]() {   // cnt[1..n] -> exclusive offsets starting at next
+        int acc = next;
+        for (int i = 0; i < n; ++i) { int c = cnt[i + 1]; cnt[i + 1] = acc; acc += c; }
+        next = acc;
+    };
+    std::vector<double> addx, addy;
+    auto grow = [&](int upto) { addx.resize(upto - base); addy.resize(upto - base); };
     // create_edgenodes: over edges (todivide element, larger neighbour)
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        int c = 0;
+        if (todiv[i])
+            for (int q = aptr[i]; q < aptr[i + 1]; ++q)
+                if (i < adj[q] && edge_of(i, adj[q]) >= 0) ++c;
+        cnt[i + 1] = c;
+    }
+    scan();
+    grow(next);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         if (!todiv[i]) continue;
+        int id = cnt[i + 1];
         for (int q = aptr[i]; q < aptr[i + 1]; ++q) {
             int k = adj[q];
             if (!(i < k)) continue;
             int j = edge_of(i, k);
             if (j < 0) continue;
-            double px, py;
-            midpoint(i, j, px, py);
-            edgenode[pairkey(i, k)] = base + (int)addx.size();
-            addx.push_back(px); addy.push_back(py);
+            midpoint(i, j, addx[id - base], addy[id - base]);
+            adjnode[q] = id;
+            int qk = slot_of(k, i);
+            if (qk >= 0) adjnode[qk] = id;
+            ++id;
         }
     }
-    // ... then under edges whose smaller neighbour is not divided (sorted by pair)
+    // ... then under edges whose smaller neighbour is not divided
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < n; ++k) {
+        int c = 0;
+        if (todiv[k])
+            for (int q = aptr[k]; q < aptr[k + 1]; ++q) {
+                int i2 = adj[q];
+                if (i2 < k && !todiv[i2] && edge_of(i2, k) >= 0) ++c;
+            }
+        cnt[k + 1] = c;
+    }
+    scan();
+    grow(next);
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < n; ++k) {
         if (!todiv[k]) continue;
+        int id = cnt[k + 1];
         for (int q = aptr[k]; q < aptr[k + 1]; ++q) {
             int i2 = adj[q];
             if (!(i2 < k) || todiv[i2]) continue;
             int j = edge_of(i2, k);
             if (j < 0) continue;
-            double px, py;
-            midpoint(i2, j, px, py);
-            edgenode[pairkey(i2, k)] = base + (int)addx.size();
-            addx.push_back(px); addy.push_back(py);
+            midpoint(i2, j, addx[id - base], addy[id - base]);
+            adjnode[q] = id;
+            int qi = slot_of(i2, k);
+            if (qi >= 0) adjnode[qi] = id;
+            ++id;
         }
     }
     // create_centernodes (mesh_utils.f90:203-230)
     std::vector<int> center(n, -1);
+    for (int i = 0; i < n; ++i) cnt[i + 1] = todiv[i] ? 1 : 0;
+    scan();
+    grow(next);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         if (!todiv[i]) continue;
         const int *v = &eind[eptr[i]];
         double px = nx[v[0]] + nx[v[1]] + nx[v[2]] + nx[v[3]];
         double py = ny[v[0]] + ny[v[1]] + ny[v[2]] + ny[v[3]];
-        center[i] = base + (int)addx.size();
-        addx.push_back(px / 4.0); addy.push_back(py / 4.0);
+        center[i] = cnt[i + 1];
+        addx[center[i] - base] = px / 4.0;
+        addy[center[i] - base] = py / 4.0;
     }
     // create_singlenodes (mesh_utils.f90:232-267): edges without a neighbour
-    std::unordered_map<uint64_t, int> single;
-    std::vector<int> nbr_on_edge((size_t)n * 4, -1);
+    std::vector<int> nbr_on_edge((size_t)n * 4, -1), single((size_t)n * 4, -1);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        int c = 0;
+        if (todiv[i]) {
+            for (int q = aptr[i]; q < aptr[i + 1]; ++q) {
+                int j = edge_of(i, adj[q]);
+                if (j >= 0 && j < 4) nbr_on_edge[(size_t)i * 4 + j] = q;   // last neighbour on the edge
+            }
+            for (int j = 0; j < 4; ++j) c += nbr_on_edge[(size_t)i * 4 + j] < 0;
+        }
+        cnt[i + 1] = c;
+    }
+    scan();
+    grow(next);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         if (!todiv[i]) continue;
-        for (int q = aptr[i]; q < aptr[i + 1]; ++q) {
-            int j = edge_of(i, adj[q]);
-            if (j >= 0 && j < 4) nbr_on_edge[(size_t)i * 4 + j] = adj[q];
-        }
+        int id = cnt[i + 1];
         for (int j = 0; j < 4; ++j) {
             if (nbr_on_edge[(size_t)i * 4 + j] >= 0) continue;
-            double px, py;
-            midpoint(i, j, px, py);
-            single[((uint64_t)i << 2) | (uint64_t)j] = base + (int)addx.size();
-            addx.push_back(px); addy.push_back(py);
+            midpoint(i, j, addx[id - base], addy[id - base]);
+            single[(size_t)i * 4 + j] = id++;
         }
     }
     // select_newhanging (mesh_utils.f90:411-452)
     std::vector<uint8_t> ishang(n, 0);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
         if (todiv[i]) continue;
         for (int q = aptr[i]; q < aptr[i + 1]; ++q)
-            if (todiv[adj[q]] && edgenode.count(pairkey(i, adj[q]))) { ishang[i] = 1; break; }
+            if (todiv[adj[q]] && adjnode[q] >= 0) { ishang[i] = 1; break; }
     }
-    // final_division (mesh_utils.f90:454-681)
-    std::vector<int> neptr{0}, neind;
-    std::vector<uint8_t> nediv;
-    std::vector<int> nemat;
-    neptr.reserve(n + 1); neind.reserve(eind.size() * 2); nediv.reserve(eind.size() * 2); nemat.reserve(n);
-    std::vector<int> aeptr{0}, aeind, aemat;
-    std::vector<uint8_t> aediv;
+    // final_division (mesh_utils.f90:454-681): kept elements in order, then
+    // per element in order its hanging version or its four children
+    std::vector<int> kptr(n + 1, 0), aslot(n + 1, 0), acnt(n + 1, 0);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
+        int kept = 0, ae = 0, an = 0;
         if (ishang[i]) {
             int toins[4] = {-1, -1, -1, -1};
-            for (int q = aptr[i]; q < aptr[i + 1]; ++q) {
-                int k = adj[q];
-                if (!todiv[k]) continue;
-                auto it = edgenode.find(pairkey(i, k));
-                if (it == edgenode.end()) continue;
-                int j = edge_of(i, k);
-                if (j >= 0 && j < 4) toins[j] = it->second;
-            }
-            const int *v = &eind[eptr[i]];
-            for (int j = 0; j < 4; ++j) {
-                aeind.push_back(v[j]); aediv.push_back(0);
-                if (toins[j] >= 0) { aeind.push_back(toins[j]); aediv.push_back(1); }
-            }
-            aeptr.push_back((int)aeind.size());
-            aemat.push_back(emat[i]);
+            for (int q = aptr[i]; q < aptr[i + 1]; ++q)
+                if (todiv[adj[q]] && adjnode[q] >= 0) {
+                    int j = edge_of(i, adj[q]);
+                    if (j >= 0 && j < 4) toins[j] = adjnode[q];
+                }
+            ae = 1;
+            an = 4;
+            for (int j = 0; j < 4; ++j) an += toins[j] >= 0;
+        } else if (todiv[i]) {
+            ae = 4;
+            an = 16;
+        } else {
+            kept = eptr[i + 1] - eptr[i];
         }
-        if (todiv[i]) {
-            int t[4];
-            for (int j = 0; j < 4; ++j) {
-                int k = nbr_on_edge[(size_t)i * 4 + j];
-                if (k < 0) t[j] = single[((uint64_t)i << 2) | (uint64_t)j];
-                else t[j] = edgenode[pairkey(i, k)];
+        kptr[i + 1] = kept;
+        aslot[i + 1] = ae;
+        acnt[i + 1] = an;
+    }
+    for (int i = 0; i < n; ++i) { kptr[i + 1] += kptr[i]; aslot[i + 1] += aslot[i]; acnt[i + 1] += acnt[i]; }
+    int nkept = 0;
+    for (int i = 0; i < n; ++i) nkept += !(ishang[i] || todiv[i]);
+    const int nel_new = nkept + aslot[n];
+    const int off = kptr[n];   // slots of the kept elements
+    std::vector<int> neptr(nel_new + 1, 0), neind((size_t)off + acnt[n]), nemat(nel_new);
+    std::vector<uint8_t> nediv((size_t)off + acnt[n], 0);
+    // kept element index = rank among kept elements
+    std::vector<int> krank(n + 1, 0);
+    for (int i = 0; i < n; ++i) krank[i + 1] = krank[i] + !(ishang[i] || todiv[i]);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        if (ishang[i] || todiv[i]) {
+            int e0 = nkept + aslot[i];
+            int o = off + acnt[i];
+            if (ishang[i]) {
+                int toins[4] = {-1, -1, -1, -1};
+                for (int q = aptr[i]; q < aptr[i + 1]; ++q) {
+                    int k = adj[q];
+                    if (!todiv[k] || adjnode[q] < 0) continue;
+                    int j = edge_of(i, k);
+                    if (j >= 0 && j < 4) toins[j] = adjnode[q];
+                }
+                const int *v = &eind[eptr[i]];
+                for (int j = 0; j < 4; ++j) {
+                    neind[o] = v[j]; nediv[o++] = 0;
+                    if (toins[j] >= 0) { neind[o] = toins[j]; nediv[o++] = 1; }
+                }
+                neptr[e0 + 1] = o;
+                nemat[e0] = emat[i];
+            } else {
+                int t[4];
+                for (int j = 0; j < 4; ++j) {
+                    int q = nbr_on_edge[(size_t)i * 4 + j];
+                    t[j] = q < 0 ? single[(size_t)i * 4 + j] : adjnode[q];
+                }
+                const int *v = &eind[eptr[i]];
+                int n1 = v[0], n2 = v[1], n3 = v[2], n4 = v[3], c = center[i];
+                // material at the parent's opposite corner (mesh_utils.f90:622-649)
+                double diff = ny[n3] - ny[n1];
+                double p[4][2] = {{nx[n1] + diff, ny[n1] + diff}, {nx[n2] - diff, ny[n2] + diff},
+                                  {nx[n3] - diff, ny[n3] - diff}, {nx[n4] + diff, ny[n4] - diff}};
+                int kids[4][4] = {{n1, t[0], c, t[3]}, {t[0], n2, t[1], c}, {c, t[1], n3, t[2]}, {t[3], c, t[2], n4}};
+                for (int q = 0; q < 4; ++q) {
+                    for (int j = 0; j < 4; ++j) { neind[o] = kids[q][j]; nediv[o++] = 0; }
+                    neptr[e0 + q + 1] = o;
+                    nemat[e0 + q] = material_prop(p[q][0], p[q][1]);
+                }
             }
-            const int *v = &eind[eptr[i]];
-            int n1 = v[0], n2 = v[1], n3 = v[2], n4 = v[3], c = center[i];
-            // material at the parent's opposite corner (mesh_utils.f90:622-649)
-            double diff = ny[n3] - ny[n1];
-            double p[4][2] = {{nx[n1] + diff, ny[n1] + diff}, {nx[n2] - diff, ny[n2] + diff},
-                              {nx[n3] - diff, ny[n3] - diff}, {nx[n4] + diff, ny[n4] - diff}};
-            int kids[4][4] = {{n1, t[0], c, t[3]}, {t[0], n2, t[1], c}, {c, t[1], n3, t[2]}, {t[3], c, t[2], n4}};
-            for (int q = 0; q < 4; ++q) {
-                for (int j = 0; j < 4; ++j) { aeind.push_back(kids[q][j]); aediv.push_back(0); }
-                aeptr.push_back((int)aeind.size());
-                aemat.push_back(material_prop(p[q][0], p[q][1]));
-            }
+        } else {
+            const int e0 = krank[i];
+            int o = kptr[i];
+            for (int j = eptr[i]; j < eptr[i + 1]; ++j) { neind[o] = eind[j]; nediv[o++] = ediv[j]; }
+            neptr[e0 + 1] = o;
+            nemat[e0] = emat[i];
         }
     }
-    for (int e = 0; e < n; ++e) {
-        if (ishang[e] || todiv[e]) continue;
-        for (int j = eptr[e]; j < eptr[e + 1]; ++j) { neind.push_back(eind[j]); nediv.push_back(ediv[j]); }
-        neptr.push_back((int)neind.size());
-        nemat.push_back(emat[e]);
-    }
-    int off = (int)neind.size();
-    for (size_t q = 1; q < aeptr.size(); ++q) neptr.push_back(off + aeptr[q]);
-    neind.insert(neind.end(), aeind.begin(), aeind.end());
-    nediv.insert(nediv.end(), aediv.begin(), aediv.end());
-    nemat.insert(nemat.end(), aemat.begin(), aemat.end());
     eptr.swap(neptr); eind.swap(neind); ediv.swap(nediv); emat.swap(nemat);
     nx.insert(nx.end(), addx.begin(), addx.end());
     ny.insert(ny.end(), addy.begin(), addy.end());

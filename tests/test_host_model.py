@@ -179,3 +179,23 @@ def test_sheet_txt_layout(tmp_path):
     rows = txt.split("FIELD = [ ")[1].split(" ];")[0].strip().split("\n")
     assert len(rows) == 3 and [float(v) for v in rows[1].split()] == list(range(4, 8))
     assert txt.rstrip().endswith("SAMP = 0.010000 ;")
+
+
+MESH_SHA = {   # sha256 of eptr, eind, ediv, nodes, ematprop, hanging, seismic, absorbing
+    "canyon": (17504, 17990, "39c7d8b3c0340a35c892167c986383769a2624065a2f1815e34d698753f27620"),
+    "valley": (137724, 139151, "b63dc9a5f188b8a89b55990e2f9ae391c31f3d63efabfe0d054500b035e3587f"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MESH_SHA))
+def test_mesher_output_is_pinned(name):
+    """The mesh (element order, node numbering, hanging list) is pinned: the
+    divide passes number new nodes in the reference's append order whatever
+    the thread count."""
+    import hashlib
+    d = decks.canyon(scale=0.3, steps=10) if name == "canyon" else decks.valley(scale=0.3, steps=10)
+    m = Model(d)
+    h = hashlib.sha256()
+    for a in (m.eptr(), m.eind(), m.ediv(), m.nodes(), m.ematprop(), m.hanging(), m.seismic(), m.absorbing()):
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert (m.nelems, m.nnodes, h.hexdigest()) == MESH_SHA[name]
