@@ -384,7 +384,8 @@ def main():
                     help="timed loop only (no autotune, kernel profile, e2e, CPU or FP64 legs): for ncu captures")
     ap.add_argument("--block", type=int, default=0, help="force the step kernel's block size")
     ap.add_argument("--rpt", type=int, default=0, help="force right-hand sides per thread")
-    ap.add_argument("--variant", type=int, default=-1, help="force the kernel variant (FP32: 0 tiled, 1 direct)")
+    ap.add_argument("--variant", type=int, default=-1, help="force the kernel variant (FP32: 0 direct gather, 1 shared-memory tiles, 2 bulk-copy "
+                         "pipeline; FP64: 0 reference order, 1 closed form)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     args = ap.parse_args()

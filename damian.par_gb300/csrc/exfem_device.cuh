@@ -140,6 +140,42 @@ __host__ __device__ __forceinline__ void planewave(const DevWave &w, double t, d
     }
 }
 
+// One term of planewave: m = 0 incident, 1 reflected P, 2 reflected SV.
+// pw_term gives the term's parts px[c], pz[c] of ux[c], uz[c] with planewave's
+// arithmetic, so planewave's ux[c] is px_0[c] + px_1[c] + px_2[c] summed in
+// that order; pw_term_u gives the displacement column alone, as planewave_u
+// computes it.  Threads evaluating the terms in parallel reproduce the
+// one-thread values bit for bit.
+__host__ __device__ __forceinline__ double pw_delay(const DevWave &w, int m, double x1, double x3) {
+    if (m == 0) {
+        if (w.kind == EXFEM_WAVE_P) return (x1 * w.sine - x3 * w.cose) / w.alpha;
+        return (x1 * w.sinf - x3 * w.cosf) / w.beta;
+    }
+    if (m == 1) return (x1 * w.sine + x3 * w.cose) / w.alpha;
+    return (x1 * w.sinf + x3 * w.cosf) / w.beta;
+}
+__host__ __device__ __forceinline__ void pw_term(const DevWave &w, int m, double t, double x1, double x3,
+                                              double px[3], double pz[3]) {
+    double r[3];
+    ricker3(w.fp, t - pw_delay(w, m, x1, x3), r);
+    const double amp = m == 0 ? w.amp0 : (m == 1 ? w.wa1 : w.wb1);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        px[c] = r[c] * w.wui[2 * m] * amp;
+        pz[c] = r[c] * w.wui[2 * m + 1] * amp;
+    }
+}
+// Displacement of one term (the column planewave_u sums).
+__host__ __device__ __forceinline__ void pw_term_u(const DevWave &w, int m, double t, double x1, double x3,
+                                                double &px, double &pz) {
+    const double q = w.fp * (t - pw_delay(w, m, x1, x3));
+    const double sq = q * q;
+    const double r = (1.0 - 2.0 * sq) / exp(sq);
+    const double amp = m == 0 ? w.amp0 : (m == 1 ? w.wa1 : w.wb1);
+    px = r * w.wui[2 * m] * amp;
+    pz = r * w.wui[2 * m + 1] * amp;
+}
+
 // Displacement column only.
 __host__ __device__ __forceinline__ void planewave_u(const DevWave &w, double t, double x1, double x3, double &ux,
                                             double &uz) {

@@ -160,25 +160,40 @@ __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile 
 // DRM forces (model.f90:745-800) for the FP32 form: travel times in FP64,
 // the Ricker terms and the boundary/exterior split in FP32.
 __global__ void k_drm32(DevModel m) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)m.ns * m.R) return;
-    int s = (int)(t / m.R), r = (int)(t % m.R);
-    int step = read_step(m) + 1;
-    const DevWave &w = m.waves[r];
-    double outt = (double)step * m.dt - w.t0;
-    int ie = m.s_elem[s];
+    // four threads per (boundary element, rhs): thread k evaluates the free
+    // field at corner k, the quad shares the values, thread k stores forces
+    // 2k and 2k+1 (launch: 4 * ns * R threads, blocks of a multiple of 4)
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = t >> 2;
+    const int k = (int)(t & 3);
+    const bool valid = w < (long long)m.ns * m.R;
+    int s = 0, r = 0, ie = 0;
+    float uk[2] = {0.f, 0.f}, ak[2] = {0.f, 0.f};
+    if (valid) {
+        s = (int)(w / m.R);
+        r = (int)(w % m.R);
+        int step = read_step(m) + 1;
+        const DevWave &wv = m.waves[r];
+        double outt = (double)step * m.dt - wv.t0;
+        ie = m.s_elem[s];
+        int x = m.econn[4 * ie + k];
+        planewave32(wv, outt, m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, uk, ak);
+    }
     float u0[8], a0[8];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        int x = m.econn[4 * ie + k];
-        planewave32(w, outt, m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, &u0[2 * k], &a0[2 * k]);
+    for (int c = 0; c < 4; ++c) {
+        u0[2 * c] = __shfl_sync(0xffffffffu, uk[0], c, 4);
+        u0[2 * c + 1] = __shfl_sync(0xffffffffu, uk[1], c, 4);
+        a0[2 * c] = __shfl_sync(0xffffffffu, ak[0], c, 4);
+        a0[2 * c + 1] = __shfl_sync(0xffffffffu, ak[1], c, 4);
     }
+    if (!valid) return;
     const float4 k4 = reinterpret_cast<const float4 *>(m.ecoef32)[ie];
     float kc[4] = {k4.x, k4.y, k4.z, k4.w};
     float p[8];
     drm_forces<float>(kc, (float)m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) m.fdrm32[((size_t)s * 8 + k) * m.R + r] = p[k];
+    m.fdrm32[((size_t)s * 8 + 2 * k) * m.R + r] = p[2 * k];
+    m.fdrm32[((size_t)s * 8 + 2 * k + 1) * m.R + r] = p[2 * k + 1];
 }
 
 // The fused step for one non-hanging node and RPT right-hand sides.  The
@@ -864,10 +879,34 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
             }
         }
     } else if (step % m.io == 0) {
-        long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
-        if (t < (long long)m.nrecv * m.R) {
-            int i = (int)(t % m.nrecv), r = (int)(t / m.nrecv);
-            int slot = step / m.io;
+        // four threads per (receiver, rhs): thread q < 3 evaluates free-field
+        // term q (the FP64 Ricker pulses are the cost), thread 0 interpolates
+        // and adds the terms in planewave_u's order
+        const long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
+        const long long wq = t >> 2;
+        const int q = (int)(t & 3);
+        const bool valid = wq < (long long)m.nrecv * m.R;
+        const int slot = step / m.io;
+        int i = 0, r = 0;
+        bool soil = false;
+        double px = 0.0, pz = 0.0;
+        if (valid) {
+            i = (int)(wq % m.nrecv);
+            r = (int)(wq / m.nrecv);
+            soil = m.rsoil[i] != 0;
+            if (soil && q < 3) {
+                const DevWave wv = m.waves[r];
+                double time = m.dt * (double)slot * (double)m.io;
+                pw_term_u(wv, q, time - wv.t0, m.rxy[2 * i] - m.worigin_x, m.rxy[2 * i + 1] - m.worigin_y, px, pz);
+            }
+        }
+        double tx[3], tz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            tx[k] = __shfl_sync(0xffffffffu, px, k, 4);
+            tz[k] = __shfl_sync(0xffffffffu, pz, k, 4);
+        }
+        if (valid && q == 0) {
             double fx = 0.0, fy = 0.0;
             for (int k = 0; k < 4; ++k) {
                 double vx, vy;
@@ -876,13 +915,10 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
                 fx += w * vx;
                 fy += w * vy;
             }
-            if (m.rsoil[i]) {
-                const DevWave wv = m.waves[r];
-                double time = m.dt * (double)slot * (double)m.io;
-                double ddx, ddz;
-                planewave_u(wv, time - wv.t0, m.rxy[2 * i] - m.worigin_x, m.rxy[2 * i + 1] - m.worigin_y, ddx, ddz);
-                fx += ddx;
-                fy += ddz;
+            if (soil) {
+                const double dx = tx[0] + tx[1] + tx[2], dz = tz[0] + tz[1] + tz[2];
+                fx = fx + dx;
+                fy = fy + dz;
             }
             size_t o = (((size_t)r * m.nsave + slot) * m.nrecv + i) * 2;
             m.seis[o] = fx;
@@ -1141,7 +1177,7 @@ int f32_launch_step(Ctx &c, int par) {
     DevModel &m = c.dm;
     float *uh = c.uhi[par], *uhn = c.uhi[par ^ 1];
     if (m.ns > 0) {
-        k_drm32<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+        k_drm32<<<nblocks(4LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
         c.launches++;
         mark(c, "k_drm32");
     }
@@ -1190,7 +1226,7 @@ int f32_launch_step(Ctx &c, int par) {
     }
     const int TH = 256;
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + TH - 1) / TH);
-    int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
+    int nbr = (int)((4LL * m.nrecv * m.R + TH - 1) / TH);   // four threads per receiver
     k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0);
     c.launches++;
     mark(c, "k_hang32");
@@ -1201,7 +1237,7 @@ int f32_launch_step(Ctx &c, int par) {
 int f32_launch_sample0(Ctx &c, int par) {
     DevModel &m = c.dm;
     const int TH = 256;
-    int nbr = (int)(((long long)m.nrecv * m.R + TH - 1) / TH);
+    int nbr = (int)((4LL * m.nrecv * m.R + TH - 1) / TH);   // four threads per receiver
     if (nbr > 0) {
         k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.uhi[par], c.ucomp, c.udel[0], c.dcomp, 0, 1);
         c.launches++;

@@ -61,41 +61,73 @@ __device__ __forceinline__ double sqm(int i, int j) {
 // One thread per (boundary element, rhs): wave_reactions with the dense
 // multdrm loops (formulation.f90:378-393).  Stores the stiffness part and
 // the mass part separately (each is added to the reactions on its own).
+// Sixteen threads per (DRM element, rhs).  Thread 4c + q evaluates term q of
+// the free field (incident, reflected P, reflected SV; q = 3 idles) at the
+// element's corner c: its FP64 Ricker pulse is the cost.  Shuffles give every
+// thread the corner values, summed term by term in planewave's order, and
+// thread o < 8 forms row o of both multdrm products.  For each row it applies
+// exactly the updates of the reference's loop over (i, j), in the same order,
+// so every force is bit for bit the one-thread result.  Launch: 16 * ns * R
+// threads, blocks of a multiple of 16.
 __global__ void k_drm_ref(DevModel m) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)m.ns * m.R) return;
-    int s = (int)(t / m.R), r = (int)(t % m.R);
-    int step = *(volatile int *)m.d_step + 1;
-    const DevWave w = m.waves[r];
-    double outt = (double)step * m.dt - w.t0;
-    int ie = m.s_elem[s];
-    double u0[8], a0[8];
-    for (int k = 0; k < 4; ++k) {
-        int x = m.econn[4 * ie + k];
-        double ox = m.nxy[2 * x] - m.worigin_x, oz = m.nxy[2 * x + 1] - m.worigin_y;
-        double ux[3], uz[3];
-        planewave(w, outt, ox, oz, ux, uz);
-        u0[2 * k] = ux[0]; u0[2 * k + 1] = uz[0];
-        a0[2 * k] = ux[2]; a0[2 * k + 1] = uz[2];
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = t >> 4;
+    const int l = (int)(t & 15), corner = l >> 2, term = l & 3;
+    const bool valid = w < (long long)m.ns * m.R;
+    int s = 0, r = 0, ie = 0;
+    double p0x = 0.0, p0z = 0.0, p2x = 0.0, p2z = 0.0;   // columns u and ddu of this term
+    if (valid) {
+        s = (int)(w / m.R);
+        r = (int)(w % m.R);
+        ie = m.s_elem[s];
+        if (term < 3) {
+            int step = *(volatile int *)m.d_step + 1;
+            const DevWave wv = m.waves[r];
+            double outt = (double)step * m.dt - wv.t0;
+            int x = m.econn[4 * ie + corner];
+            double ox = m.nxy[2 * x] - m.worigin_x, oz = m.nxy[2 * x + 1] - m.worigin_y;
+            double px[3], pz[3];
+            pw_term(wv, term, outt, ox, oz, px, pz);
+            p0x = px[0]; p0z = pz[0];
+            p2x = px[2]; p2z = pz[2];
+        }
     }
+    double u0[8], a0[8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        double v[4][3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            v[0][q] = __shfl_sync(0xffffffffu, p0x, 4 * c + q, 16);
+            v[1][q] = __shfl_sync(0xffffffffu, p0z, 4 * c + q, 16);
+            v[2][q] = __shfl_sync(0xffffffffu, p2x, 4 * c + q, 16);
+            v[3][q] = __shfl_sync(0xffffffffu, p2z, 4 * c + q, 16);
+        }
+        u0[2 * c] = v[0][0] + v[0][1] + v[0][2];
+        u0[2 * c + 1] = v[1][0] + v[1][1] + v[1][2];
+        a0[2 * c] = v[2][0] + v[2][1] + v[2][2];
+        a0[2 * c + 1] = v[3][0] + v[3][1] + v[3][2];
+    }
+    if (!valid || l >= 8) return;
+    const int o = l;
     unsigned e = drm_mask(m.s_kind[s]);
     double K[64];
     calck(m.emulam[2 * ie], m.emulam[2 * ie + 1], K);
-    double pk[8], pm[8];
-    for (int i = 0; i < 8; ++i) { pk[i] = 0.0; pm[i] = 0.0; }
+    double pk = 0.0, pm = 0.0;
     for (int i = 0; i < 8; ++i)
         for (int j = 0; j < 8; ++j)
             if (((e >> j) & 1u) && !((e >> i) & 1u)) {
-                pk[i] = pk[i] - K[j * 8 + i] * u0[j];
-                pk[j] = pk[j] + K[i * 8 + j] * u0[i];
-                pm[i] = pm[i] - sqm(i, j) * a0[j];
-                pm[j] = pm[j] + sqm(j, i) * a0[i];
+                if (i == o) {
+                    pk = pk - K[j * 8 + o] * u0[j];
+                    pm = pm - sqm(o, j) * a0[j];
+                }
+                if (j == o) {
+                    pk = pk + K[i * 8 + o] * u0[i];
+                    pm = pm + sqm(o, i) * a0[i];
+                }
             }
-    double mass = m.emass[ie];
-    for (int k = 0; k < 8; ++k) {
-        m.fdrm[((size_t)s * 16 + k) * m.R + r] = pk[k];
-        m.fdrm[((size_t)s * 16 + 8 + k) * m.R + r] = pm[k] * mass;
-    }
+    m.fdrm[((size_t)s * 16 + o) * m.R + r] = pk;
+    m.fdrm[((size_t)s * 16 + 8 + o) * m.R + r] = pm * m.emass[ie];
 }
 
 __global__ void __launch_bounds__(128) k_elem_ref(DevModel m, const double *__restrict__ u,
@@ -220,10 +252,34 @@ __global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict
                 unew[((size_t)h * 2 + d) * R + r] = (unew[((size_t)a * 2 + d) * R + r] + unew[((size_t)b * 2 + d) * R + r]) / 2.0;
         }
     } else if (step % m.io == 0) {
-        long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
-        if (t < (long long)m.nrecv * m.R) {
-            int i = (int)(t % m.nrecv), r = (int)(t / m.nrecv);
-            int slot = step / m.io;
+        // four threads per (receiver, rhs): thread q < 3 evaluates free-field
+        // term q (the FP64 Ricker pulses are the cost), thread 0 interpolates
+        // and adds the terms in planewave_u's order
+        const long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
+        const long long wq = t >> 2;
+        const int q = (int)(t & 3);
+        const bool valid = wq < (long long)m.nrecv * m.R;
+        const int slot = step / m.io;
+        int i = 0, r = 0;
+        bool soil = false;
+        double px = 0.0, pz = 0.0;
+        if (valid) {
+            i = (int)(wq % m.nrecv);
+            r = (int)(wq / m.nrecv);
+            soil = m.rsoil[i] != 0;
+            if (soil && q < 3) {
+                const DevWave wv = m.waves[r];
+                double time = m.dt * (double)slot * (double)m.io;
+                pw_term_u(wv, q, time - wv.t0, m.rxy[2 * i] - m.worigin_x, m.rxy[2 * i + 1] - m.worigin_y, px, pz);
+            }
+        }
+        double tx[3], tz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            tx[k] = __shfl_sync(0xffffffffu, px, k, 4);
+            tz[k] = __shfl_sync(0xffffffffu, pz, k, 4);
+        }
+        if (valid && q == 0) {
             double fx = 0.0, fy = 0.0;
             for (int k = 0; k < 4; ++k) {
                 double vx, vy;
@@ -232,11 +288,8 @@ __global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict
                 fx = fx + w * vx;
                 fy = fy + w * vy;
             }
-            if (m.rsoil[i]) {
-                const DevWave wv = m.waves[r];
-                double time = m.dt * (double)slot * (double)m.io;
-                double dx, dz;
-                planewave_u(wv, time - wv.t0, m.rxy[2 * i] - m.worigin_x, m.rxy[2 * i + 1] - m.worigin_y, dx, dz);
+            if (soil) {
+                const double dx = tx[0] + tx[1] + tx[2], dz = tz[0] + tz[1] + tz[2];
                 fx = fx + dx;
                 fy = fy + dz;
             }
@@ -269,7 +322,7 @@ int f64ref_launch_drm_elem_node(Ctx &c, int par) {
     double *u = c.u64[par], *um = c.u64[par ^ 1];
     const int T = 128;
     if (m.ns > 0) {
-        k_drm_ref<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+        k_drm_ref<<<nblocks(16LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
         c.launches++;
         mark(c, "k_drm_ref");
     }
@@ -286,7 +339,7 @@ int f64_launch_hang(Ctx &c, double *unew, int mode) {
     DevModel &m = c.dm;
     const int T = 128;
     int nbh = mode == 1 ? 0 : (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);
-    int nbr = (int)(((long long)m.nrecv * m.R + T - 1) / T);
+    int nbr = (int)((4LL * m.nrecv * m.R + T - 1) / T);   // four threads per receiver
     if (nbh + nbr == 0) return EXFEM_OK;
     k_hang_ref<<<nbh + nbr, T, 0, c.stream>>>(m, unew, nbh, mode);
     c.launches++;
@@ -374,7 +427,7 @@ extern "C" int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_
     double *ef = base + ef_off;
     const int T = 128;
     k_noalloc_prep<<<1, 1, 0, c.stream>>>(counters, step);
-    if (m.ns > 0) k_drm_ref<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+    if (m.ns > 0) k_drm_ref<<<nblocks(16LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
     k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, d_u, d_um, ef);
     k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, ef, d_unew);
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);

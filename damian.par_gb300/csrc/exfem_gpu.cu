@@ -47,31 +47,46 @@ thread_local std::string g_create_err;
 __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
 
 // ---------------------------------------------------------------- DRM ----
-// One thread per (boundary element, rhs).  Free field at the element's four
-// corners, then multdrm for K and for the consistent mass (model.f90:766-798).
+// Free field at a boundary element's four corners, then multdrm for K and for
+// the consistent mass (model.f90:766-798), in closed form.  Four threads per
+// (boundary element, rhs): thread k evaluates the free field at corner k, the
+// quad shares the values by shuffles, thread k stores forces 2k and 2k+1
+// (launch: 4 * ns * R threads, blocks of a multiple of 4).
 __global__ void k_drm(DevModel m) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)m.ns * m.R) return;
-    int s = (int)(t / m.R), r = (int)(t % m.R);
-    int step = read_step(m) + 1;
-    const DevWave w = m.waves[r];
-    double outt = (double)step * m.dt - w.t0;   // timetransform(m_wttoorigin, i*dt)
-    int ie = m.s_elem[s];
-    double u0[8], a0[8];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long w = t >> 2;
+    const int k = (int)(t & 3);
+    const bool valid = w < (long long)m.ns * m.R;
+    int s = 0, r = 0, ie = 0;
+    double ukx = 0.0, ukz = 0.0, akx = 0.0, akz = 0.0;
+    if (valid) {
+        s = (int)(w / m.R);
+        r = (int)(w % m.R);
+        int step = read_step(m) + 1;
+        const DevWave wv = m.waves[r];
+        double outt = (double)step * m.dt - wv.t0;   // timetransform(m_wttoorigin, i*dt)
+        ie = m.s_elem[s];
         int x = m.econn[4 * ie + k];
         double ox = m.nxy[2 * x] - m.worigin_x, oz = m.nxy[2 * x + 1] - m.worigin_y;
         double ux[3], uz[3];
-        planewave(w, outt, ox, oz, ux, uz);
-        u0[2 * k] = ux[0]; u0[2 * k + 1] = uz[0];
-        a0[2 * k] = ux[2]; a0[2 * k + 1] = uz[2];
+        planewave(wv, outt, ox, oz, ux, uz);
+        ukx = ux[0]; ukz = uz[0];
+        akx = ux[2]; akz = uz[2];
     }
+    double u0[8], a0[8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        u0[2 * c] = __shfl_sync(0xffffffffu, ukx, c, 4);
+        u0[2 * c + 1] = __shfl_sync(0xffffffffu, ukz, c, 4);
+        a0[2 * c] = __shfl_sync(0xffffffffu, akx, c, 4);
+        a0[2 * c + 1] = __shfl_sync(0xffffffffu, akz, c, 4);
+    }
+    if (!valid) return;
     double kc[4] = {m.ecoef[4 * ie], m.ecoef[4 * ie + 1], m.ecoef[4 * ie + 2], m.ecoef[4 * ie + 3]};
     double p[8];
     drm_forces<double>(kc, m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) m.fdrm[((size_t)s * 16 + k) * m.R + r] = p[k];
+    m.fdrm[((size_t)s * 16 + 2 * k) * m.R + r] = p[2 * k];
+    m.fdrm[((size_t)s * 16 + 2 * k + 1) * m.R + r] = p[2 * k + 1];
 }
 
 // ----------------------------------------------------------- elements ----
@@ -240,7 +255,7 @@ int launch_step64(Ctx &c, int par) {
     } else {
         const int T = c.block_threads;
         if (m.ns > 0) {
-            k_drm<<<nblocks((long long)m.ns * m.R, 64), 64, 0, c.stream>>>(m);
+            k_drm<<<nblocks(4LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
             c.launches++;
             mark(c, "k_drm");
         }
