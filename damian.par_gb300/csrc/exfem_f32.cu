@@ -942,8 +942,8 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
 
 inline int nblocks(long long work, int threads) { return (int)std::max<long long>(1, (work + threads - 1) / threads); }
 
-template <typename T>
-int upload32(Ctx &c, const std::vector<T> &v, const T **dst) {
+template <typename T, typename A>
+int upload32(Ctx &c, const std::vector<T, A> &v, const T **dst) {
     if (v.empty()) { *dst = nullptr; return EXFEM_OK; }
     void *p = nullptr;
     CK(cudaMalloc(&p, v.size() * sizeof(T)));
@@ -1057,7 +1057,7 @@ int f32_alloc(Ctx &c) {
     const Plan &P = c.plan;
     DevModel &m = c.dm;
     // per active node: 1/m_full (x, y), -2 a2 C (x, y)
-    const std::vector<float> nc = node_coef32(P);
+    const pvec<float> nc = node_coef32(P);
     std::vector<float> hc((size_t)4 * std::max(P.n_hang, 1), 0.f);
     for (int i = 0; i < P.n_hang; ++i) {
         int h = P.hang[3 * (size_t)i];
@@ -1142,7 +1142,9 @@ int f32_alloc(Ctx &c) {
     // the direct gather's per-term corner copies
     m.tcorn = nullptr;
     if (!c.use_tiles && !c.use_pipe) {
-        std::vector<int> tc(4 * std::max<size_t>(P.tlist.size(), 1), 0);
+        pvec<int> tc;
+        tc.resize(4 * std::max<size_t>(P.tlist.size(), 1));
+        if (P.tlist.empty()) std::fill(tc.begin(), tc.end(), 0);
         const long long nt = (long long)P.tlist.size();
 #pragma omp parallel for schedule(static)
         for (long long q = 0; q < nt; ++q) {

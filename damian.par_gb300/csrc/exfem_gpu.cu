@@ -275,8 +275,8 @@ int launch_sample0_64(Ctx &c, int par) {
     return EXFEM_OK;
 }
 
-template <typename T>
-int upload(Ctx &c, const std::vector<T> &v, const T **dst) {
+template <typename T, typename A>
+int upload(Ctx &c, const std::vector<T, A> &v, const T **dst) {
     if (v.empty()) { *dst = nullptr; return EXFEM_OK; }
     void *p = nullptr;
     CK(cudaMalloc(&p, v.size() * sizeof(T)));

@@ -27,9 +27,10 @@ uint64_t spread21(uint64_t v) {
 
 struct Morton {
     double x0, y0, sx, sy;
-    Morton(const std::vector<double> &xs, const std::vector<double> &ys) {
+    Morton(const double *xs, const double *ys, long long n) {
         double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
-        for (size_t i = 0; i < xs.size(); ++i) {
+#pragma omp parallel for schedule(static) reduction(min : xmin, ymin) reduction(max : xmax, ymax)
+        for (long long i = 0; i < n; ++i) {
             xmin = std::min(xmin, xs[i]); xmax = std::max(xmax, xs[i]);
             ymin = std::min(ymin, ys[i]); ymax = std::max(ymax, ys[i]);
         }
@@ -119,54 +120,121 @@ int init_wave_const(const exfem_wave &w, double alpha, double beta, WaveConst &o
     return EXFEM_OK;
 }
 
-// Stable LSD radix sort of the ids in idx by key[id]: 11-bit digits, so a
+// Inclusive prefix sum in place over a[0..n).  Two passes over fixed chunks:
+// integer sums, so the result is exact whatever the thread count.
+static void scan_inclusive(int *a, long long n) {
+    constexpr int NCH = 64;
+    if (n < (1 << 16)) {
+        for (long long i = 1; i < n; ++i) a[i] += a[i - 1];
+        return;
+    }
+    const long long chunk = (n + NCH - 1) / NCH;
+    long long part[NCH + 1] = {0};
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < NCH; ++t) {
+        const long long lo = t * chunk, hi = std::min(n, lo + chunk);
+        long long s = 0;
+        for (long long i = lo; i < hi; ++i) s += a[i];
+        part[t + 1] = s;
+    }
+    for (int t = 0; t < NCH; ++t) part[t + 1] += part[t];
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < NCH; ++t) {
+        const long long lo = t * chunk, hi = std::min(n, lo + chunk);
+        int s = (int)part[t];
+        for (long long i = lo; i < hi; ++i) {
+            s += a[i];
+            a[i] = s;
+        }
+    }
+}
+
+// CSR pointers from per-row counts: ptr[0] = 0 and ptr[i + 1] holds row i's
+// count on entry, the row start sums on return.
+static void counts_to_ptr(pvec<int> &ptr) {
+    ptr[0] = 0;
+    if (ptr.size() > 1) scan_inclusive(ptr.data() + 1, (long long)ptr.size() - 1);
+}
+
+// The ids i in [0, n) with keep(i) true, in increasing order (parallel
+// stream compaction over fixed chunks).
+template <class F>
+static void compact_ids(int n, F keep, pvec<int> &out) {
+    constexpr int NCH = 64;
+    const int chunk = (n + NCH - 1) / NCH;
+    int part[NCH + 1] = {0};
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < NCH; ++t) {
+        const int lo = std::min(n, t * chunk), hi = std::min(n, lo + chunk);
+        int c = 0;
+        for (int i = lo; i < hi; ++i) c += keep(i) ? 1 : 0;
+        part[t + 1] = c;
+    }
+    for (int t = 0; t < NCH; ++t) part[t + 1] += part[t];
+    out.resize(part[NCH]);
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < NCH; ++t) {
+        const int lo = std::min(n, t * chunk), hi = std::min(n, lo + chunk);
+        int o = part[t];
+        for (int i = lo; i < hi; ++i)
+            if (keep(i)) out[o++] = i;
+    }
+}
+
+// Stable LSD radix sort of the ids idx[0..n) by key[id]: 11-bit digits, so a
 // pass's 2048 scatter streams stay in cache; a pass whose digit is the same
-// for every key is skipped.  Each pass splits the array into fixed chunks that
-// count and scatter in parallel, with offsets laid out digit-major then
-// chunk-major, so the result is the stable order whatever the thread count.
-// Sorts contiguous (key, id) pairs so every pass streams through memory.
-static void radix_order(const std::vector<uint64_t> &key, std::vector<int> &idx) {
-    const long long n = (long long)idx.size();
+// for every key is skipped.  Each pass splits the array into chunks that count
+// (into a local histogram) and scatter in parallel; the offsets are laid out
+// digit-major then chunk-major, so the result is the stable order whatever
+// the chunk or thread count.  Sorts contiguous (key, id) records so every pass
+// streams through memory.
+struct KeyId {
+    uint64_t key;
+    int id;
+};
+static void radix_order(const uint64_t *key, int *idx, long long n) {
     if (n < 2) return;
     constexpr int BITS = 11;
-    constexpr size_t NB = size_t(1) << BITS;
-    constexpr int NCH = 64;   // chunks per pass
-    const long long chunk = (n + NCH - 1) / NCH;
-    std::vector<std::pair<uint64_t, int>> a(n), b(n);
+    constexpr int NB = 1 << BITS;
+    const int nch = (int)std::min<long long>(64, std::max<long long>(1, n / 16384));   // chunks per pass
+    const long long chunk = (n + nch - 1) / nch;
+    pvec<KeyId> a, b;
+    a.resize(n);
+    b.resize(n);
     uint64_t any = 0, all = ~0ull;
 #pragma omp parallel for schedule(static) reduction(| : any) reduction(& : all)
     for (long long i = 0; i < n; ++i) {
         a[i] = {key[idx[i]], idx[i]};
-        any |= a[i].first;
-        all &= a[i].first;
+        any |= a[i].key;
+        all &= a[i].key;
     }
-    std::vector<size_t> hist((size_t)NCH * NB);
+    std::vector<long long> off((size_t)NB * nch);   // [digit][chunk]
     for (int sh = 0; sh < 64; sh += BITS) {
         if ((((any ^ all) >> sh) & (NB - 1)) == 0) continue;
 #pragma omp parallel for schedule(static, 1)
-        for (int t = 0; t < NCH; ++t) {
-            size_t *h = &hist[(size_t)t * NB];
-            std::fill(h, h + NB, 0);
+        for (int t = 0; t < nch; ++t) {
+            long long h[NB] = {0};
             const long long lo = t * chunk, hi = std::min(n, lo + chunk);
-            for (long long i = lo; i < hi; ++i) h[(a[i].first >> sh) & (NB - 1)]++;
+            for (long long i = lo; i < hi; ++i) h[(a[i].key >> sh) & (NB - 1)]++;
+            for (int d = 0; d < NB; ++d) off[(size_t)d * nch + t] = h[d];
         }
-        size_t off = 0;
-        for (size_t d = 0; d < NB; ++d)
-            for (int t = 0; t < NCH; ++t) {
-                const size_t c = hist[(size_t)t * NB + d];
-                hist[(size_t)t * NB + d] = off;
-                off += c;
-            }
+        long long run = 0;
+        for (size_t i = 0; i < off.size(); ++i) {
+            const long long c = off[i];
+            off[i] = run;
+            run += c;
+        }
 #pragma omp parallel for schedule(static, 1)
-        for (int t = 0; t < NCH; ++t) {
-            size_t *h = &hist[(size_t)t * NB];
+        for (int t = 0; t < nch; ++t) {
+            long long h[NB];
+            for (int d = 0; d < NB; ++d) h[d] = off[(size_t)d * nch + t];
             const long long lo = t * chunk, hi = std::min(n, lo + chunk);
-            for (long long i = lo; i < hi; ++i) b[h[(a[i].first >> sh) & (NB - 1)]++] = a[i];
+            for (long long i = lo; i < hi; ++i) b[h[(a[i].key >> sh) & (NB - 1)]++] = a[i];
         }
         a.swap(b);
     }
 #pragma omp parallel for schedule(static)
-    for (long long i = 0; i < n; ++i) idx[i] = a[i].second;
+    for (long long i = 0; i < n; ++i) idx[i] = a[i].id;
 }
 
 int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &P, std::string &err) {
@@ -215,24 +283,52 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     P.worigin[0] = prob.worigin[0];
     P.worigin[1] = prob.worigin[1];
 
-    // ---- corners (elemallnhnodes, model.f90:163-174) and validation
+    // ---- corners (elemallnhnodes, model.f90:163-174) and validation.  The
+    // checks run in parallel; the first failing element (lowest id) is then
+    // checked again alone for its message.
     if (mesh.eptr[0] != 1) { err = "eptr[0] must be 1 (1-based CSR)"; return EXFEM_E_MESH; }
-    std::vector<int> corner_ref((size_t)ne * 4);
-    for (int e = 0; e < ne; ++e) {
-        int b = mesh.eptr[e] - 1, t = mesh.eptr[e + 1] - 1;
-        if (t <= b || t - b > 8) { err = "element " + std::to_string(e + 1) + " has a bad CSR row"; return EXFEM_E_MESH; }
+    pvec<int> corner_ref;
+    corner_ref.resize((size_t)ne * 4);
+    auto check_elem = [&](int e, std::string *msg) -> bool {
+        const int b = mesh.eptr[e] - 1, t = mesh.eptr[e + 1] - 1;
+        if (t <= b || t - b > 8) {
+            if (msg) *msg = "element " + std::to_string(e + 1) + " has a bad CSR row";
+            return false;
+        }
         int k = 0;
         for (int j = b; j < t; ++j) {
-            int v = mesh.eind[j];
-            if (v < 1 || v > nn) { err = "eind out of range in element " + std::to_string(e + 1); return EXFEM_E_MESH; }
-            if (!mesh.ediv[j]) { if (k < 4) corner_ref[(size_t)e * 4 + k] = v - 1; ++k; }
+            const int v = mesh.eind[j];
+            if (v < 1 || v > nn) {
+                if (msg) *msg = "eind out of range in element " + std::to_string(e + 1);
+                return false;
+            }
+            if (!mesh.ediv[j]) {
+                if (k < 4) corner_ref[(size_t)e * 4 + k] = v - 1;
+                ++k;
+            }
         }
         if (k != 4) {
-            err = "element " + std::to_string(e + 1) + " has " + std::to_string(k) + " non-hanging nodes (model.f90:166-171)";
+            if (msg)
+                *msg = "element " + std::to_string(e + 1) + " has " + std::to_string(k) +
+                       " non-hanging nodes (model.f90:166-171)";
+            return false;
+        }
+        const int m = mesh.ematprop[e];
+        if (m < 1 || m > prob.nmat) {
+            if (msg) *msg = "ematprop out of range in element " + std::to_string(e + 1);
+            return false;
+        }
+        return true;
+    };
+    {
+        int first_bad = ne;
+#pragma omp parallel for schedule(static) reduction(min : first_bad)
+        for (int e = 0; e < ne; ++e)
+            if (!check_elem(e, nullptr)) first_bad = std::min(first_bad, e);
+        if (first_bad < ne) {
+            check_elem(first_bad, &err);
             return EXFEM_E_MESH;
         }
-        int m = mesh.ematprop[e];
-        if (m < 1 || m > prob.nmat) { err = "ematprop out of range in element " + std::to_string(e + 1); return EXFEM_E_MESH; }
     }
     // ---- hanging entries
     std::vector<int> hang_of(nn, -1);   // reference node -> hanging entry
@@ -255,31 +351,39 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         }
     }
     // ---- internal numbering (Morton order; active nodes first, hanging last)
-    std::vector<double> xs(nn), ys(nn);
+    pvec<double> xs, ys;
+    xs.resize(nn);
+    ys.resize(nn);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nn; ++i) { xs[i] = mesh.nodes[2 * i]; ys[i] = mesh.nodes[2 * i + 1]; }
     // active nodes in Morton order (stable), then hanging entry i as node n_active + i
-    std::vector<int> order;
-    order.reserve(nn);
-    for (int i = 0; i < nn; ++i)
-        if (hang_of[i] < 0) order.push_back(i);
-    Morton mort(xs, ys);
-    if (reorder) {
-        std::vector<uint64_t> keys(nn, 0);
-#pragma omp parallel for schedule(static)
-        for (int i = 0; i < nn; ++i) keys[i] = mort.key(xs[i], ys[i]);
-        radix_order(keys, order);
-    }
-    for (int i = 0; i < prob.nhanging; ++i) order.push_back(prob.hanging[3 * i] - 1);
-    P.ref_of_node = order;
-    P.node_of_ref.assign(nn, -1);
-    for (int i = 0; i < nn; ++i) P.node_of_ref[order[i]] = i;
     P.n_hang = prob.nhanging;
     P.n_active = nn - P.n_hang;
-
-    std::vector<int> eorder(ne);
-    std::iota(eorder.begin(), eorder.end(), 0);
+    pvec<int> &order = P.ref_of_node;
+    order.reserve(nn);
+    compact_ids(nn, [&](int i) { return hang_of[i] < 0; }, order);
+    Morton mort(xs.data(), ys.data(), nn);
     if (reorder) {
-        std::vector<uint64_t> ek(ne);
+        pvec<uint64_t> keys;
+        keys.resize(nn);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < nn; ++i) keys[i] = mort.key(xs[i], ys[i]);
+        radix_order(keys.data(), order.data(), (long long)order.size());
+    }
+    order.resize(nn);
+    for (int i = 0; i < prob.nhanging; ++i) order[(size_t)P.n_active + i] = prob.hanging[3 * i] - 1;
+    // every reference node appears once in order: the scatter sets each entry
+    P.node_of_ref.resize(nn);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nn; ++i) P.node_of_ref[order[i]] = i;
+
+    pvec<int> &eorder = P.ref_of_elem;
+    eorder.resize(ne);
+#pragma omp parallel for schedule(static)
+    for (int e = 0; e < ne; ++e) eorder[e] = e;
+    if (reorder) {
+        pvec<uint64_t> ek;
+        ek.resize(ne);
 #pragma omp parallel for schedule(static)
         for (int e = 0; e < ne; ++e) {
             const int *c = &corner_ref[(size_t)e * 4];
@@ -287,10 +391,11 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             double cy = 0.25 * (ys[c[0]] + ys[c[1]] + ys[c[2]] + ys[c[3]]);
             ek[e] = mort.key(cx, cy);
         }
-        radix_order(ek, eorder);
+        radix_order(ek.data(), eorder.data(), ne);
     }
-    P.ref_of_elem = eorder;
-    std::vector<int> elem_of_ref(ne);
+    pvec<int> &elem_of_ref = P.elem_of_ref;   // kept for point sampling
+    elem_of_ref.resize(ne);
+#pragma omp parallel for schedule(static)
     for (int e = 0; e < ne; ++e) elem_of_ref[eorder[e]] = e;
 
     // ---- per-element data (internal order); dashpot slots numbered in that order
@@ -299,10 +404,11 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     P.ecoef32.resize((size_t)ne * 4);
     P.emass.resize(ne);
     P.emulam.resize((size_t)ne * 2);
-    P.edamp.assign(ne, -1);
     P.edampv.clear();
-    std::vector<double> eh(ne);
-    std::vector<char> damped(ne, 0);
+    pvec<double> eh;
+    eh.resize(ne);
+    pvec<char> damped;
+    damped.resize(ne);
     int bad_elem = ne;   // first element (reference id) with a bad length or density
 #pragma omp parallel for schedule(static) reduction(min : bad_elem)
     for (int ie = 0; ie < ne; ++ie) {
@@ -312,6 +418,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         const double *mc = &prob.matconst[5 * (mesh.ematprop[e] - 1)];
         double mu = mc[0], lam = mc[1], rho = mc[2];
         double h = ys[c[2]] - ys[c[0]];   // elength (model.f90:112-118)
+        damped[ie] = 0;
         if (!(h > 0) || !(rho > 0)) { bad_elem = std::min(bad_elem, e); continue; }
         eh[ie] = h;
         P.emulam[(size_t)ie * 2] = mu;
@@ -333,9 +440,14 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         return EXFEM_E_MESH;
     }
     {
-        int nd = 0;
-        for (int ie = 0; ie < ne; ++ie)
-            if (damped[ie]) P.edamp[ie] = nd++;
+        // dashpot slot of element ie: the damped elements before it
+        P.edamp.resize(ne);
+#pragma omp parallel for schedule(static)
+        for (int ie = 0; ie < ne; ++ie) P.edamp[ie] = damped[ie];
+        scan_inclusive(P.edamp.data(), ne);
+        const int nd = P.edamp[ne - 1];
+#pragma omp parallel for schedule(static)
+        for (int ie = 0; ie < ne; ++ie) P.edamp[ie] = damped[ie] ? P.edamp[ie] - 1 : -1;
         P.edampv.assign((size_t)nd * 8, 0.0);
 #pragma omp parallel for schedule(static)
         for (int ie = 0; ie < ne; ++ie) {
@@ -355,28 +467,55 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             }
         }
     }
-    // ---- own incidences per node (internal ids), reference element order
-    P.ownptr.assign(nn + 1, 0);
-    for (int ie = 0; ie < ne; ++ie)
-        for (int k = 0; k < 4; ++k) P.ownptr[P.econn[(size_t)ie * 4 + k] + 1]++;
-    for (int i = 0; i < nn; ++i) P.ownptr[i + 1] += P.ownptr[i];
+    // ---- own incidences per node (internal ids) in reference element order:
+    // counted and placed in parallel, then each node's few entries are sorted
+    // by (reference element, corner), the order the element loop adds them
+    const long long ncorn = 4LL * ne;
+    P.ownptr.resize((size_t)nn + 1);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i <= nn; ++i) P.ownptr[i] = 0;
+#pragma omp parallel for schedule(static)
+    for (long long j = 0; j < ncorn; ++j) __atomic_fetch_add(&P.ownptr[(size_t)P.econn[j] + 1], 1, __ATOMIC_RELAXED);
+    counts_to_ptr(P.ownptr);
     P.ownlist.resize(P.ownptr[nn]);
     {
-        std::vector<int> fill(P.ownptr.begin(), P.ownptr.end() - 1);
-        for (int e = 0; e < ne; ++e) {   // reference element order
-            int ie = elem_of_ref[e];
-            for (int k = 0; k < 4; ++k) P.ownlist[fill[P.econn[(size_t)ie * 4 + k]]++] = ie * 4 + k;
+        pvec<int> fill;
+        fill.resize(nn);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < nn; ++i) fill[i] = P.ownptr[i];
+#pragma omp parallel for schedule(static)
+        for (long long j = 0; j < ncorn; ++j) {
+            const int s = __atomic_fetch_add(&fill[P.econn[j]], 1, __ATOMIC_RELAXED);
+            P.ownlist[s] = (int)j;
+        }
+        auto order_key = [&](int v) { return eorder[v >> 2] * 4 + (v & 3); };
+#pragma omp parallel for schedule(static)
+        for (int x = 0; x < nn; ++x) {
+            int *l = &P.ownlist[P.ownptr[x]];
+            const int cnt = P.ownptr[x + 1] - P.ownptr[x];
+            for (int i = 1; i < cnt; ++i) {
+                const int v = l[i], kv = order_key(v);
+                int j = i - 1;
+                while (j >= 0 && order_key(l[j]) > kv) { l[j + 1] = l[j]; --j; }
+                l[j + 1] = v;
+            }
         }
     }
-    for (int i = 0; i < nn; ++i)
-        if (P.ownptr[i + 1] == P.ownptr[i]) {
-            err = "node " + std::to_string(P.ref_of_node[i] + 1) + " is not a non-hanging corner of any element";
+    {
+        int first_lonely = nn;
+#pragma omp parallel for schedule(static) reduction(min : first_lonely)
+        for (int i = 0; i < nn; ++i)
+            if (P.ownptr[i + 1] == P.ownptr[i]) first_lonely = std::min(first_lonely, i);
+        if (first_lonely < nn) {
+            err = "node " + std::to_string(P.ref_of_node[first_lonely] + 1) + " is not a non-hanging corner of any element";
             return EXFEM_E_MESH;
         }
+    }
     // ---- m_full (init_explicit, explicit.f90:95-106): each dof sums its
     // element terms in reference element order (the incidence lists' order),
-    // as the element loop adds them; then sum_reactanchors in halving form
-    P.mfull_ref.assign((size_t)2 * nn, 0.0);
+    // as the element loop adds them; then sum_reactanchors in halving form.
+    // ref_of_node is a permutation, so the loop sets every entry.
+    P.mfull_ref.resize((size_t)2 * nn);
 #pragma omp parallel for schedule(static)
     for (int n = 0; n < nn; ++n) {
         const size_t x = (size_t)P.ref_of_node[n];
@@ -403,16 +542,26 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     }
     P.inv_mfull.resize((size_t)2 * P.n_active);
     P.mfull_int.resize((size_t)2 * P.n_active);
-    for (int n = 0; n < P.n_active; ++n)
-        for (int k = 0; k < 2; ++k) {
-            double m = P.mfull_ref[(size_t)P.ref_of_node[n] * 2 + k];
-            if (!(m > 0)) { err = "non-positive lumped mass at node " + std::to_string(P.ref_of_node[n] + 1); return EXFEM_E_MESH; }
-            P.inv_mfull[(size_t)2 * n + k] = 1.0 / m;
-            P.mfull_int[(size_t)2 * n + k] = m;
+    {
+        int first_bad = P.n_active;
+#pragma omp parallel for schedule(static) reduction(min : first_bad)
+        for (int n = 0; n < P.n_active; ++n)
+            for (int k = 0; k < 2; ++k) {
+                double m = P.mfull_ref[(size_t)P.ref_of_node[n] * 2 + k];
+                if (!(m > 0)) first_bad = std::min(first_bad, n);
+                P.inv_mfull[(size_t)2 * n + k] = 1.0 / m;
+                P.mfull_int[(size_t)2 * n + k] = m;
+            }
+        if (first_bad < P.n_active) {
+            err = "non-positive lumped mass at node " + std::to_string(P.ref_of_node[first_bad] + 1);
+            return EXFEM_E_MESH;
         }
+    }
     // ---- hanging entries (internal) and per-anchor links (h, other anchor), entry order
     P.hang.resize((size_t)3 * P.n_hang);
-    P.lptr.assign(P.n_active + 1, 0);
+    P.lptr.resize((size_t)P.n_active + 1);
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n <= P.n_active; ++n) P.lptr[n] = 0;
     for (int i = 0; i < prob.nhanging; ++i) {
         int h = P.node_of_ref[prob.hanging[3 * i] - 1];
         int a = P.node_of_ref[prob.hanging[3 * i + 1] - 1];
@@ -421,10 +570,13 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         P.lptr[a + 1]++;
         P.lptr[b + 1]++;
     }
-    for (int n = 0; n < P.n_active; ++n) P.lptr[n + 1] += P.lptr[n];
+    counts_to_ptr(P.lptr);
     P.llist.assign(2 * (size_t)P.lptr[P.n_active], 0);
-    {
-        std::vector<int> fill(P.lptr.begin(), P.lptr.end() - 1);
+    if (prob.nhanging > 0) {
+        pvec<int> fill;
+        fill.resize(P.n_active);
+#pragma omp parallel for schedule(static)
+        for (int n = 0; n < P.n_active; ++n) fill[n] = P.lptr[n];
         for (int i = 0; i < prob.nhanging; ++i) {
             int h = P.hang[3 * (size_t)i], a = P.hang[3 * (size_t)i + 1], b = P.hang[3 * (size_t)i + 2];
             int qa = fill[a]++, qb = fill[b]++;
@@ -433,7 +585,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         }
     }
     // ---- gather lists of active nodes: own terms, then linked hanging terms at 1/2
-    P.tptr.assign(P.n_active + 1, 0);
+    P.tptr.resize((size_t)P.n_active + 1);
 #pragma omp parallel for schedule(static)
     for (int n = 0; n < P.n_active; ++n) {
         int cnt = P.ownptr[n + 1] - P.ownptr[n];
@@ -443,8 +595,8 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         }
         P.tptr[n + 1] = cnt;
     }
-    for (int n = 0; n < P.n_active; ++n) P.tptr[n + 1] += P.tptr[n];
-    P.tlist.assign(P.tptr[P.n_active], 0);
+    counts_to_ptr(P.tptr);
+    P.tlist.resize(P.tptr[P.n_active]);
 #pragma omp parallel for schedule(static)
     for (int n = 0; n < P.n_active; ++n) {
         int o = P.tptr[n];
@@ -455,8 +607,8 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         }
     }
     // ---- per-node lumped mass / damping (internal), for the FP32 increment form
-    P.nmass.assign(nn, 0.0);
-    P.ndamp.assign((size_t)2 * nn, 0.0);
+    P.nmass.resize(nn);
+    P.ndamp.resize((size_t)2 * nn);
 #pragma omp parallel for schedule(static)
     for (int x = 0; x < nn; ++x) {
         double ms = 0.0, d0 = 0.0, d1 = 0.0;
@@ -497,26 +649,35 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             }
         }
     }
-    P.odptr.assign(nn + 1, 0);
+    P.odptr.resize((size_t)nn + 1);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i <= nn; ++i) P.odptr[i] = 0;
     for (int s = 0; s < prob.nseismic; ++s)
         for (int k = 0; k < 4; ++k) P.odptr[P.econn[(size_t)P.s_elem[s] * 4 + k] + 1]++;
-    for (int i = 0; i < nn; ++i) P.odptr[i + 1] += P.odptr[i];
+    counts_to_ptr(P.odptr);
     P.odlist.resize(P.odptr[nn]);
-    {
-        std::vector<int> fill(P.odptr.begin(), P.odptr.end() - 1);
+    if (prob.nseismic > 0) {
+        pvec<int> fill;
+        fill.resize(nn);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < nn; ++i) fill[i] = P.odptr[i];
         for (int s = 0; s < prob.nseismic; ++s)
             for (int k = 0; k < 4; ++k) P.odlist[fill[P.econn[(size_t)P.s_elem[s] * 4 + k]]++] = s * 4 + k;
     }
-    P.dptr.assign(P.n_active + 1, 0);
+    P.dptr.resize((size_t)P.n_active + 1);
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n <= P.n_active; ++n) P.dptr[n] = 0;
     for (auto &de : dent) P.dptr[de.first + 1]++;
-    for (int n = 0; n < P.n_active; ++n) P.dptr[n + 1] += P.dptr[n];
-    P.dlist.assign(P.dptr[P.n_active], 0);
-    {
-        std::vector<int> fill(P.dptr.begin(), P.dptr.end() - 1);
+    counts_to_ptr(P.dptr);
+    P.dlist.resize(P.dptr[P.n_active]);
+    if (!dent.empty()) {
+        pvec<int> fill;
+        fill.resize(P.n_active);
+#pragma omp parallel for schedule(static)
+        for (int n = 0; n < P.n_active; ++n) fill[n] = P.dptr[n];
         for (auto &de : dent) P.dlist[fill[de.first]++] = de.second;
     }
-    // ---- kept for point sampling
-    P.elem_of_ref = elem_of_ref;
+    // ---- kept for point sampling (elem_of_ref above): internal node coordinates
     P.nxy.resize(2 * (size_t)nn);
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < nn; ++i) {
@@ -643,8 +804,10 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
     return EXFEM_OK;
 }
 
-std::vector<float> node_coef32(const Plan &P) {
-    std::vector<float> nc((size_t)4 * P.n_active);
+pvec<float> node_coef32(const Plan &P) {
+    pvec<float> nc;
+    nc.resize((size_t)4 * P.n_active);
+#pragma omp parallel for schedule(static)
     for (int n = 0; n < P.n_active; ++n) {
         nc[4 * (size_t)n] = (float)P.inv_mfull[2 * (size_t)n];
         nc[4 * (size_t)n + 1] = (float)P.inv_mfull[2 * (size_t)n + 1];
@@ -659,7 +822,7 @@ bool build_pipe_pack(const Plan &P, const Tiles &T, int max_runs, PipePack &out,
     if (T.hmax >= (1 << 14)) { why = "tile halo over 16383 nodes"; return false; }
     if (P.dlist.size() >= (1u << 24) || P.llist.size() / 2 >= (1u << 24)) { why = "DRM or link list over 2^24"; return false; }
     auto fbits = [](float f) { int i; std::memcpy(&i, &f, sizeof(i)); return i; };
-    const std::vector<float> nc = node_coef32(P);
+    const pvec<float> nc = node_coef32(P);
     const int tn = T.tn;
     out.hdr.assign(4 * (size_t)T.ntiles, 0);
     out.runs.assign(2 * (size_t)max_runs * T.ntiles, 0);

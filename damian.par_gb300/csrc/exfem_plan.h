@@ -9,12 +9,36 @@
 #pragma once
 
 #include <cstdint>
+#include <new>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "exfem_gpu.h"
 
 namespace exfem {
+
+// Allocator whose no-argument construct leaves trivial elements unset, so
+// resizing a large plan array does not zero it on one thread before the
+// parallel loop that writes every element (first touch then happens on the
+// threads that fill it).
+template <class T>
+struct RawAlloc : std::allocator<T> {
+    template <class U>
+    struct rebind { using other = RawAlloc<U>; };
+    RawAlloc() = default;
+    template <class U>
+    RawAlloc(const RawAlloc<U> &) {}
+    template <class U>
+    void construct(U *p) noexcept(std::is_nothrow_default_constructible<U>::value) { ::new (static_cast<void *>(p)) U; }
+    template <class U, class... A>
+    void construct(U *p, A &&...a) { ::new (static_cast<void *>(p)) U(std::forward<A>(a)...); }
+};
+// Plan arrays: resize() leaves new elements unset; assign() and the
+// initialiser forms still set them.
+template <class T>
+using pvec = std::vector<T, RawAlloc<T>>;
 
 // Constants of one plane wave after initplanewaves (pwaves.f90:16-98).
 struct WaveConst {
@@ -34,25 +58,25 @@ struct Plan {
     int n_hang = 0;                 // hanging nodes are internal [n_active, nn)
     double dt = 0, a1 = 0, a2 = 0, a3 = 0;
     int nsteps = 0, io = 1, nsave = 1;
-    std::vector<int> ref_of_node;   // internal -> reference node (0-based)
-    std::vector<int> node_of_ref;   // reference -> internal
-    std::vector<int> ref_of_elem;   // internal -> reference element (0-based)
+    pvec<int> ref_of_node;          // internal -> reference node (0-based)
+    pvec<int> node_of_ref;          // reference -> internal
+    pvec<int> ref_of_elem;          // internal -> reference element (0-based)
     // elements (internal order)
-    std::vector<int> econn;         // 4 per element: internal node ids of the non-hanging corners
-    std::vector<double> ecoef;      // 4 per element: (lam+2mu)/4, lam/4, mu/4, (lam+3mu)/12
-    std::vector<float> ecoef32;     // same, FP32
-    std::vector<double> emulam;     // 2 per element: (mu, lambda) for calck in reference order
-    std::vector<double> emass;      // rho*(h/2)^2 per element (getmassof)
-    std::vector<int> edamp;         // per element: index into edampv or -1
+    pvec<int> econn;                // 4 per element: internal node ids of the non-hanging corners
+    pvec<double> ecoef;             // 4 per element: (lam+2mu)/4, lam/4, mu/4, (lam+3mu)/12
+    pvec<float> ecoef32;            // same, FP32
+    pvec<double> emulam;            // 2 per element: (mu, lambda) for calck in reference order
+    pvec<double> emass;             // rho*(h/2)^2 per element (getmassof)
+    pvec<int> edamp;                // per element: index into edampv or -1
     std::vector<double> edampv;     // 8 per damped element (getdampingof)
     // gather lists for active nodes; entry = ((elem*4 + corner) << 1) | half
-    std::vector<int> tptr, tlist;
-    std::vector<int> dptr, dlist;   // DRM: ((slot*4 + corner) << 1) | half
-    std::vector<double> mfull_ref;  // m_full in reference dof order (mass.bin)
-    std::vector<double> inv_mfull;  // 2 per active node (internal), 1/m_full
-    std::vector<double> mfull_int;  // 2 per active node (internal), m_full
+    pvec<int> tptr, tlist;
+    pvec<int> dptr, dlist;          // DRM: ((slot*4 + corner) << 1) | half
+    pvec<double> mfull_ref;         // m_full in reference dof order (mass.bin)
+    pvec<double> inv_mfull;         // 2 per active node (internal), 1/m_full
+    pvec<double> mfull_int;         // 2 per active node (internal), m_full
     // per node lumped terms (internal): M_n, C_n(x,y), D_n(x,y) = a1 M + a2 C, for the FP32 form
-    std::vector<double> nmass, ndamp;
+    pvec<double> nmass, ndamp;
     // hanging entries (internal ids): h, a, b; hanging node of entry i is
     // internal node n_active + i
     std::vector<int> hang;
@@ -68,8 +92,8 @@ struct Plan {
     int nrecv = 0;
     // kept for point sampling after setup: reference -> internal element,
     // internal node coordinates, the DRM box (left, right, top)
-    std::vector<int> elem_of_ref;
-    std::vector<double> nxy;
+    pvec<int> elem_of_ref;
+    pvec<double> nxy;
     double wbox[3] = {0, 0, 0};
     // waves (have_waves false: zero-amplitude placeholders, no free field)
     std::vector<WaveConst> waves;
@@ -80,12 +104,12 @@ struct Plan {
     std::vector<unsigned char> pflag;
     double worigin[2] = {0, 0};
     // per active node: hanging links (h, other anchor) in m_hanging order
-    std::vector<int> lptr, llist;   // llist entries: h internal, b internal (pairs)
+    pvec<int> lptr, llist;          // llist entries: h internal, b internal (pairs)
     // own incidences of every node (incl. hanging): elem*4+corner, sorted by
     // reference element index (the order explicit.f90:129-142 adds them)
-    std::vector<int> ownptr, ownlist;
+    pvec<int> ownptr, ownlist;
     // own DRM incidences of every node: slot*4+corner in seismic order
-    std::vector<int> odptr, odlist;
+    pvec<int> odptr, odlist;
 };
 
 // visu_field's interpolation data (visualization.f90:156-181) for npt points
@@ -115,7 +139,7 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err);
 
 // Per active node, the FP32 step's node coefficients: 1/m_full (x, y) and
 // -2 a2 C (x, y).
-std::vector<float> node_coef32(const Plan &P);
+pvec<float> node_coef32(const Plan &P);
 
 // What the bulk-copy pipeline reads per tile, in the formats its kernel
 // decodes (all arrays of 32-bit words, every tile's part 16-byte aligned):

@@ -29,8 +29,8 @@ def lib():
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     if not os.path.exists(OUT) or os.path.getmtime(OUT) < max(os.path.getmtime(f) for f in DEPS):
         tmp = OUT + ".tmp%d" % os.getpid()
-        cmd = [NVCC, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(REPO, "include"),
-               "-I", os.path.join(PKG, "csrc"), *SRC, "-o", tmp]
+        cmd = [NVCC, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fopenmp",
+               "-I", os.path.join(REPO, "include"), "-I", os.path.join(PKG, "csrc"), *SRC, "-o", tmp, "-lgomp"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(res.stderr)
@@ -53,6 +53,7 @@ def lib():
     L.probe_plan.restype = C.c_void_p
     L.probe_plan.argtypes = [C.POINTER(Mesh), C.POINTER(Problem), C.c_int]
     L.probe_plan_free.argtypes = [C.c_void_p]
+    L.probe_set_threads.argtypes = [C.c_int]
     L.probe_plan_size.restype = C.c_longlong
     L.probe_plan_size.argtypes = [C.c_void_p, C.c_char_p]
     L.probe_plan_copy.restype = C.c_int
@@ -73,7 +74,9 @@ def dp(a):
 
 
 INT_FIELDS = {"ref_of_node", "node_of_ref", "ref_of_elem", "econn", "edamp", "tptr", "tlist", "dptr", "dlist",
-              "hang", "s_elem", "s_kind", "rnode", "rsoil", "lptr", "llist", "ownptr", "ownlist"}
+              "hang", "s_elem", "s_kind", "rnode", "rsoil", "lptr", "llist", "ownptr", "ownlist", "elem_of_ref",
+              "odptr", "odlist"}
+FLOAT32_FIELDS = {"ecoef32"}
 
 
 class PlanView:
@@ -93,7 +96,7 @@ class PlanView:
         n = L.probe_plan_size(self.h, name.encode())
         if n < 0:
             raise AttributeError(name)
-        dtype = np.int32 if name in INT_FIELDS else np.float64
+        dtype = np.int32 if name in INT_FIELDS else (np.float32 if name in FLOAT32_FIELDS else np.float64)
         out = np.zeros(max(n, 1), dtype=dtype)
         L.probe_plan_copy(self.h, name.encode(), out.ctypes.data_as(C.c_void_p))
         out = out[:n]
