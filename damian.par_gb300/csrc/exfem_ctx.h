@@ -77,6 +77,8 @@ struct Ctx {
     DevModel dm{};
     std::vector<void *> allocs;
     size_t bytes = 0;
+    // bytes copied host -> device and device -> host so far
+    unsigned long long h2d_bytes = 0, d2h_bytes = 0;
     // FP64 state: u[2] ping-pong + element forces
     double *u64[2] = {nullptr, nullptr};
     double *ef64 = nullptr;

@@ -950,6 +950,7 @@ int upload32(Ctx &c, const std::vector<T, A> &v, const T **dst) {
     c.allocs.push_back(p);
     c.bytes += v.size() * sizeof(T);
     CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    c.h2d_bytes += v.size() * sizeof(T);
     *dst = static_cast<const T *>(p);
     return EXFEM_OK;
 }
@@ -1255,6 +1256,7 @@ int f32_get_u(Ctx &c, int rhs, std::vector<double> &out) {
     std::vector<unsigned short> co(nst);
     CK(cudaMemcpy(hi.data(), c.uhi[c.parity], nst * sizeof(float), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(co.data(), c.ucomp, nst * sizeof(unsigned short), cudaMemcpyDeviceToHost));
+    c.d2h_bytes += nst * (sizeof(float) + sizeof(unsigned short));
     out.resize((size_t)P.nn * 2);
     for (int i = 0; i < P.nn; ++i)
         for (int d = 0; d < 2; ++d) {

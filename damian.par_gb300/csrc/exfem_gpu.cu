@@ -283,6 +283,7 @@ int upload(Ctx &c, const std::vector<T, A> &v, const T **dst) {
     c.allocs.push_back(p);
     c.bytes += v.size() * sizeof(T);
     CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    c.h2d_bytes += v.size() * sizeof(T);
     *dst = static_cast<const T *>(p);
     return EXFEM_OK;
 }
@@ -313,16 +314,25 @@ int setup_device(Ctx &c) {
     m.worigin_x = P.worigin[0]; m.worigin_y = P.worigin[1];
     TRY(upload(c, P.econn, &m.econn));
     TRY(upload(c, P.emass, &m.emass));
-    TRY(upload(c, P.emulam, &m.emulam));
-    TRY(upload(c, P.mfull_int, &m.mfull));
-    TRY(upload(c, P.ownptr, &m.ownptr));
-    TRY(upload(c, P.ownlist, &m.ownlist));
-    TRY(upload(c, P.odptr, &m.odptr));
-    TRY(upload(c, P.odlist, &m.odlist));
+    // arrays only the FP64 kernels read (the FP32 step folds mass, damping
+    // and the operator into its own per-node and per-term arrays)
+    m.emulam = nullptr; m.mfull = nullptr; m.ownptr = nullptr; m.ownlist = nullptr;
+    m.odptr = nullptr; m.odlist = nullptr; m.edamp = nullptr; m.edampv = nullptr;
+    m.ecoef = nullptr; m.inv_mfull = nullptr;
+    if (c.precision == EXFEM_FP64) {
+        TRY(upload(c, P.emulam, &m.emulam));
+        TRY(upload(c, P.mfull_int, &m.mfull));
+        TRY(upload(c, P.ownptr, &m.ownptr));
+        TRY(upload(c, P.ownlist, &m.ownlist));
+        TRY(upload(c, P.odptr, &m.odptr));
+        TRY(upload(c, P.odlist, &m.odlist));
+        TRY(upload(c, P.edamp, &m.edamp));
+        TRY(upload(c, P.edampv, &m.edampv));
+        TRY(upload(c, P.ecoef, &m.ecoef));
+        TRY(upload(c, P.inv_mfull, &m.inv_mfull));
+    }
     TRY(upload(c, P.lptr, &m.lptr));
     TRY(upload(c, P.llist, &m.llist));
-    TRY(upload(c, P.edamp, &m.edamp));
-    TRY(upload(c, P.edampv, &m.edampv));
     TRY(upload(c, P.tptr, &m.tptr));
     TRY(upload(c, P.tlist, &m.tlist));
     TRY(upload(c, P.dptr, &m.dptr));
@@ -334,8 +344,6 @@ int setup_device(Ctx &c) {
     TRY(upload(c, P.rw, &m.rw));
     TRY(upload(c, P.rsoil, &m.rsoil));
     TRY(upload(c, P.rxy, &m.rxy));
-    TRY(upload(c, P.ecoef, &m.ecoef));
-    TRY(upload(c, P.inv_mfull, &m.inv_mfull));
     std::vector<DevWave> dw(P.R);
     for (int r = 0; r < P.R; ++r) {
         const WaveConst &w = P.waves[r];
@@ -593,6 +601,7 @@ int exfem_gpu_sync(exfem_ctx *ctx) {
     CK(cudaStreamSynchronize(c.stream));
     int flag = 0;
     CK(cudaMemcpy(&flag, c.dm.d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    c.d2h_bytes += sizeof(int);
     if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
     if (flag & 2) { c.err = "a bounded device wait timed out"; return EXFEM_E_TIMEOUT; }
     return EXFEM_OK;
@@ -607,6 +616,7 @@ int exfem_gpu_query(exfem_ctx *ctx) {
     if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
     int flag = 0;
     CK(cudaMemcpy(&flag, c.dm.d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    c.d2h_bytes += sizeof(int);
     if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
     return EXFEM_OK;
 }
@@ -622,6 +632,7 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     if (c.precision == EXFEM_FP64) {
         std::vector<double> all((size_t)P.nn * 2 * P.R);
         CK(cudaMemcpy(all.data(), c.u64[c.parity], all.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        c.d2h_bytes += all.size() * sizeof(double);
         in.resize((size_t)P.nn * 2);
         for (int i = 0; i < P.nn; ++i)
             for (int d = 0; d < 2; ++d) in[2 * (size_t)i + d] = all[((size_t)i * 2 + d) * P.R + rhs];
@@ -648,6 +659,7 @@ int exfem_gpu_get_seismograms(exfem_ctx *ctx, double *out, size_t cap, int *nsav
     CK(cudaSetDevice(c.device));
     CK(cudaStreamSynchronize(c.stream));
     if (need) CK(cudaMemcpy(out, c.dm.seis, need * sizeof(double), cudaMemcpyDeviceToHost));
+    c.d2h_bytes += need * sizeof(double);
     return EXFEM_OK;
 }
 
@@ -757,6 +769,8 @@ int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *x
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, 16 * n, cudaMemcpyDeviceToHost, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     cudaFree(buf);
+    c.h2d_bytes += n * (32 + 16 + 16 + 4);
+    c.d2h_bytes += n * 16;
     if (e != cudaSuccess) { c.err = std::string("sample_points: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
     return EXFEM_OK;
 }
@@ -764,6 +778,13 @@ int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *x
 int exfem_gpu_steps_done(const exfem_ctx *ctx) { return ctx ? ctx->steps_done : 0; }
 long long exfem_gpu_launch_count(const exfem_ctx *ctx) { return ctx ? ctx->launches : 0; }
 size_t exfem_gpu_device_bytes(const exfem_ctx *ctx) { return ctx ? ctx->bytes : 0; }
+
+int exfem_gpu_copy_bytes(const exfem_ctx *ctx, unsigned long long *h2d, unsigned long long *d2h) {
+    if (!ctx) return EXFEM_E_ARG;
+    if (h2d) *h2d = ctx->h2d_bytes;
+    if (d2h) *d2h = ctx->d2h_bytes;
+    return EXFEM_OK;
+}
 
 size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts) {
     // An upper bound of what exfem_gpu_create and init_explicit allocate
@@ -778,9 +799,13 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
         for (size_t i = 0; i < nn; ++i) nabs += prob->absorbing[i] != 0;
     const bool f64 = !opts || opts->precision == EXFEM_FP64;
     size_t b = 16 * nn;                                            // node coordinates
-    b += ne * (16 + 8 + 16 + 4 + 32 + 16);                         // conn, mass, (mu,l), damp slot, coef, own list
-    b += 64 * std::min(ne, 4 * nabs + 4);                          // dashpot values of boundary elements
-    b += 4 * (nn + 1) * 4 + 16 * nn + 16 * nh + 12 * nh;           // node lists, m_full, 1/m_full, links, hanging
+    b += ne * (16 + 8);                                            // conn, mass
+    if (f64) {
+        b += ne * (16 + 4 + 32 + 16);                              // (mu,l), damp slot, coef, own list
+        b += 64 * std::min(ne, 4 * nabs + 4);                      // dashpot values of boundary elements
+        b += 2 * 4 * (nn + 1) + 32 * nn;                           // own and DRM-own pointers, m_full, 1/m_full
+    }
+    b += 3 * 4 * (nn + 1) + 16 * nh + 12 * nh;                     // link, gather and DRM pointers, links, hanging
     b += 4 * (4 * ne + 4 * nh);                                    // gather lists (own + hanging halves)
     b += ns * (16 + 8 + 32) + nr * (16 + 32 + 4 + 16) + R * 192;   // DRM lists, receivers, waves
     b += 16 * std::max(ns, (size_t)1) * R * 8;                      // DRM forces

@@ -91,6 +91,12 @@ class Solver:
     def device_bytes(self):
         return self.lib.exfem_gpu_device_bytes(self.h)
 
+    def copy_bytes(self):
+        """(host -> device, device -> host) bytes the context has copied so far."""
+        h2d, d2h = C.c_ulonglong(), C.c_ulonglong()
+        self._check(self.lib.exfem_gpu_copy_bytes(self.h, C.byref(h2d), C.byref(d2h)))
+        return int(h2d.value), int(d2h.value)
+
     def kernel_times(self, steps):
         """{kernel name: mean ms per launch} over `steps` steps run without a
         graph (CUDA events between launches on the context's stream)."""

@@ -238,6 +238,11 @@ long long exfem_gpu_launch_count(const exfem_ctx *ctx);
 /* Bytes of device memory held by the context. */
 size_t exfem_gpu_device_bytes(const exfem_ctx *ctx);
 
+/* Bytes the context has copied host -> device (the model's arrays at create,
+ * sample points) and device -> host (seismograms, fields, status flags) so
+ * far.  Either pointer may be NULL. */
+int exfem_gpu_copy_bytes(const exfem_ctx *ctx, unsigned long long *h2d, unsigned long long *d2h);
+
 /* Estimated device bytes a context for this mesh/problem/opts would hold
  * (used for admission by HBM footprint).  No device work. */
 size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *prob,

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from exfem import decks, workloads
-from exfem.abi import EXFEM_E_NOMEM, EXFEM_E_UNSUPPORTED, EXFEM_FP32_KAHAN
+from exfem.abi import EXFEM_E_NOMEM, EXFEM_E_UNSUPPORTED, EXFEM_FP32_KAHAN, EXFEM_FP64
 from exfem.gpu import Solver, estimate_bytes
 from exfem.model import Model
 from exfem.serve import Server, run_stream
@@ -67,6 +67,39 @@ def test_admission_respects_the_hbm_budget():
     spans = [(r["t_admit"], r["t_done"], r["reserved_bytes"]) for r in res]
     for t, _, _ in spans:
         assert sum(b for a, d, b in spans if a <= t < d) <= budget
+
+
+def test_estimate_bounds_every_form_and_copies_are_counted():
+    """Admission reserves exfem_gpu_estimate_bytes: it must bound what every
+    precision and kernel variant holds, without reserving much more.  The
+    context's copy counters see the model upload and the seismogram read."""
+    cases = [("canyon", dict(scale=0.2, steps=20)), ("valley_batched", dict(scale=0.1, steps=20)),
+             ("point_source", dict(scale=0.5, steps=20, kind="POINTN"))]
+    for name, kw in cases:
+        m = workloads.build(name, **kw)
+        held64 = None
+        for prec, variants in ((EXFEM_FP64, (0, 1)), (EXFEM_FP32_KAHAN, (0, 1, 2))):
+            for v in variants:
+                est = estimate_bytes(m, precision=prec, variant=v)
+                s = Solver(m, precision=prec, variant=v)
+                s.init_explicit()
+                h2d0, d2h0 = s.copy_bytes()
+                s.run(4)
+                seis = s.seismograms()
+                h2d1, d2h1 = s.copy_bytes()
+                held = s.device_bytes
+                s.close()
+                assert est >= held > 0, (name, prec, v, est, held)
+                if v == 0 or prec == EXFEM_FP64:
+                    # the FP32 tile variants reserve a worst-case halo
+                    assert est <= 1.3 * held + (1 << 20), (name, prec, v, est, held)
+                assert h2d0 > 0 and h2d1 == h2d0
+                assert d2h1 - d2h0 >= seis.nbytes
+                if prec == EXFEM_FP64 and v == 0:
+                    held64 = held
+                if prec == EXFEM_FP32_KAHAN and v == 0 and m.problem.nrhs == 1:
+                    # no FP64-only arrays (element operator, own lists, 1/m_full) in an FP32 context
+                    assert held < held64
 
 
 def test_failures_stay_isolated():
