@@ -115,6 +115,7 @@ struct Ctx {
     int graph_parity = -1;
     int block_threads = 128;
     int rhs_per_thread = 1;
+    bool idx32 = true;   // k_step32 with 32-bit indices (every index below 2^32)
     std::string err;
     // per-launch event marks while exfem_gpu_profile_kernels runs
     bool prof_on = false;

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "exfem_ctx.h"
@@ -199,18 +200,35 @@ __global__ void k_drm32(DevModel m) {
 // The fused step for one non-hanging node and RPT right-hand sides.  The
 // corners of each term's element come from the per-term copy m.tcorn, loaded
 // beside the term itself (not from econn after it), so the gather chain is
-// term -> corner u_hi.
-template <int RPT>
+// term -> corner u_hi.  I32: every thread id and array index fits in 32 bits
+// (checked on the host), so the index arithmetic is 32-bit and a power-of-two
+// thread count per node splits by shift and mask; this kernel is sensitive to
+// its instruction count (64-bit indices cost 7% on the 64-RHS valley).
+template <int RPT, bool I32>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
                                                 unsigned short *__restrict__ dc) {
+    using I = typename std::conditional<I32, unsigned, size_t>::type;
     const int G = m.R / RPT;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)m.n_active * G) return;
-    const int n = (int)(t / G);
-    const int r0 = (int)(t % G) * RPT;
-    const size_t R = m.R;
-    const size_t bn = ((size_t)n * 2) * R + r0;
+    int n, r0;
+    if (I32) {
+        const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+        if (t >= (unsigned)m.n_active * (unsigned)G) return;
+        if ((G & (G - 1)) == 0) {
+            n = (int)(t >> (__ffs(G) - 1));
+            r0 = (int)(t & (unsigned)(G - 1)) * RPT;
+        } else {
+            n = (int)(t / (unsigned)G);
+            r0 = (int)(t % (unsigned)G) * RPT;
+        }
+    } else {
+        const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        if (t >= (long long)m.n_active * G) return;
+        n = (int)(t / G);
+        r0 = (int)(t % G) * RPT;
+    }
+    const I R = m.R;
+    const I bn = ((I)n * 2) * R + r0;
     // Ask L2 for this node's own streaming state (read only after the
     // gather) so its DRAM latency overlaps the gather instead of following
     // it.  Measured on the 64-RHS valley: 8% faster at 4 and 1 right-hand
@@ -233,7 +251,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         int ent = __ldg(m.dlist + q);
         float w = (ent & 1) ? 0.5f : 1.0f;
         int sc = ent >> 1;
-        size_t b = ((size_t)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
+        I b = ((I)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
         float fx[RPT], fy[RPT];
         Vec<RPT>::load_cg(m.fdrm32 + b, fx);
         Vec<RPT>::load_cg(m.fdrm32 + b + R, fy);
@@ -253,7 +271,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         float ux[4][RPT], uy[4][RPT];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            size_t b = ((size_t)cc[v] * 2) * R + r0;
+            I b = ((I)cc[v] * 2) * R + r0;
             Vec<RPT>::load(uh + b, ux[v]);
             Vec<RPT>::load(uh + b + R, uy[v]);
         }
@@ -284,7 +302,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
         int h = __ldg(m.llist + 2 * q);
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
-        size_t bh = ((size_t)h * 2) * R + r0;
+        I bh = ((I)h * 2) * R + r0;
         float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
         Vec<RPT>::load_cg(dh + bh, hx);
         Vec<RPT>::load_cg(dh + bh + R, hy);
@@ -1099,6 +1117,15 @@ int f32_alloc(Ctx &c) {
         }
     }
     c.rhs_per_thread = pick_rpt(c);
+    {
+        // 32-bit indices in k_step32: thread ids (grid rounded up to a block)
+        // and the largest state and DRM-force element index
+        const unsigned long long lim = 1ull << 32;
+        const unsigned long long threads = (unsigned long long)P.n_active * (P.R / c.rhs_per_thread) + 1024;
+        const unsigned long long state = (unsigned long long)P.nn * 2 * P.R;
+        const unsigned long long drm = (unsigned long long)std::max(m.ns, 1) * 8 * P.R;
+        c.idx32 = c.opts.index_bits != 64 && threads < lim && state < lim && drm < lim;
+    }
     if (c.opts.block_threads <= 0) c.block_threads = 256;
     // shared-memory tiles (variant 1; variant 0, the default, is the direct gather)
     c.use_tiles = false;
@@ -1213,10 +1240,18 @@ int f32_launch_step(Ctx &c, int par) {
         mark(c, "k_tile32");
     } else {
     const int nb = nblocks(work, T);
-    switch (rpt) {
-        case 4: k_step32<4><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-        case 2: k_step32<2><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-        default: k_step32<1><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+    if (c.idx32) {
+        switch (rpt) {
+            case 4: k_step32<4, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            case 2: k_step32<2, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            default: k_step32<1, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        }
+    } else {
+        switch (rpt) {
+            case 4: k_step32<4, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            case 2: k_step32<2, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            default: k_step32<1, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+        }
     }
     c.launches++;
     mark(c, "k_step32");

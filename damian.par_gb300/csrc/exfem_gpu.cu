@@ -468,6 +468,7 @@ void exfem_gpu_default_opts(exfem_opts *o) {
     o->reorder = 1;
     o->check_every = 0;
     o->variant = EXFEM_VARIANT_REFERENCE_ORDER;
+    o->index_bits = 0;
 }
 
 int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts, exfem_ctx **out) {
@@ -482,6 +483,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
         g_create_err = "unknown kernel variant";
         return EXFEM_E_ARG;
     }
+    if (o.index_bits != 0 && o.index_bits != 64) { g_create_err = "index_bits must be 0 or 64"; return EXFEM_E_ARG; }
     const int max_bt = o.precision == EXFEM_FP64 ? 256 : 512;   // the kernels' __launch_bounds__
     if (o.block_threads < 0 || o.block_threads > max_bt || (o.block_threads % 32) != 0) {
         g_create_err = "block_threads must be a multiple of 32 in [0, " + std::to_string(max_bt) + "]";

@@ -135,6 +135,9 @@ typedef struct exfem_opts {
                           streamed by bulk copies through a two-stage
                           shared-memory pipeline (persistent grid; needs nrhs
                           a multiple of 4, else the direct gather runs)       */
+    int index_bits;    /* FP32 direct gather: 0 = 32-bit indices when every
+                          thread id and array index fits, else 64; 64 = always
+                          64-bit (same results)                               */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;

@@ -121,6 +121,29 @@ def test_tiled_and_direct_kernels_agree():
         assert np.array_equal(ua[r], ub[r]), r
 
 
+@pytest.mark.parametrize("rpt", [4, 2, 1])
+def test_32_and_64_bit_indices_agree(rpt):
+    """k_step32's 32-bit index form (shift and mask thread split) and its
+    64-bit form compute the same terms in the same order: the same state bit
+    for bit, on a batched valley with hanging nodes and a DRM layer; and a
+    thread count per node that is not a power of two (12 RHS) takes the
+    division path."""
+    m = workloads.build("valley_batched", scale=0.1, steps=60, save_every=2)
+    assert m.problem.nhanging > 0 and m.problem.nseismic > 0 and m.problem.nrhs == 64
+    a, ua = run32(m, variant=0, rhs_per_thread=rpt)
+    b, ub = run32(m, variant=0, rhs_per_thread=rpt, index_bits=64)
+    assert np.array_equal(a, b)
+    for r in range(m.problem.nrhs):
+        assert np.array_equal(ua[r], ub[r]), r
+    m12 = workloads.build("canyon", scale=0.2, steps=60, save_every=2, waves=EIGHT_WAVES + EIGHT_WAVES[:4])
+    assert m12.problem.nrhs == 12
+    a, ua = run32(m12, variant=0, rhs_per_thread=rpt)
+    b, ub = run32(m12, variant=0, rhs_per_thread=rpt, index_bits=64)
+    assert np.array_equal(a, b)
+    for r in range(m12.problem.nrhs):
+        assert np.array_equal(ua[r], ub[r]), r
+
+
 EIGHT_WAVES = [("WAVEP", 0.0), ("WAVEP", 20.0), ("WAVEP", 40.0), ("WAVEP", 60.0),
                ("WAVESV", 0.0), ("WAVESV", 10.0), ("WAVESV", 20.0), ("WAVESV", 25.0)]
 
