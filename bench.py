@@ -324,19 +324,22 @@ def run_ours(args, ws, rank, local, dist, torch):
     # run + seismogram read-back
     e2e_steps = args.steps
     me = workloads.build(args.workload, scale=args.scale, steps=e2e_steps)
-    t0 = time.perf_counter()
-    se = Solver(me, precision=form, device=local, **tuned)
-    se.init_explicit()
-    se.run(e2e_steps)
-    seis = se.seismograms()
-    h2d, d2h = se.copy_bytes()
-    se.close()
-    t_e2e = time.perf_counter() - t0
+    t_req = []
+    for _ in range(3):   # three requests; the median is reported
+        t0 = time.perf_counter()
+        se = Solver(me, precision=form, device=local, **tuned)
+        se.init_explicit()
+        se.run(e2e_steps)
+        seis = se.seismograms()
+        h2d, d2h = se.copy_bytes()
+        se.close()
+        t_req.append(time.perf_counter() - t0)
+    t_e2e = sorted(t_req)[1]
     e2e = {"value": ws * me.nelems * R * e2e_steps / t_e2e, "unit": "elem-steps*rhs/s",
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "input_bytes": input_bytes(me),
-           "seismogram_bytes": int(seis.nbytes),
+           "seismogram_bytes": int(seis.nbytes), "request_s": [round(t, 4) for t in t_req],
            "note": "one request per bench step: create (host plan + uploads) + init_explicit + %d steps + "
-                   "seismograms; byte counts are the context's own host<->device copies" % e2e_steps}
+                   "seismograms, median of 3; byte counts are the context's own host<->device copies" % e2e_steps}
 
     # the plain FP64 form on the same workload, for the FP32 / FP64 ratio
     fp64_ref = None
