@@ -220,6 +220,49 @@ def serving_leg(args, local):
     return summary
 
 
+def saturated_serving_leg(args, local):
+    """Server capacity: a burst of requests sized like the serving config
+    (canyons and valleys of 3e4-9e5 elements, 1-16 angles) submitted at once,
+    meshed before the clock, so the server stays saturated.  Served
+    element-steps*RHS/s = total work / makespan (plan builds, uploads,
+    admission and stepping included).  The plain FP64 GPU form is timed on
+    every request (CUDA events over 10 steps after 3) and its throughput is
+    the same total work over the sum of steps x ms/step."""
+    from exfem import decks
+    from exfem.gpu import Solver
+    from exfem.model import Model
+    from exfem.serve import Server
+    stream = decks.serving_stream(n=args.serve_burst, rate=1e9, seed=5, min_scale=0.3, max_scale=1.0,
+                                  max_angles=16, step_range=(1000, 2000), canyon_nperlen=25.0, valley_chper=0.07)
+    reqs = [(Model(d, nsteps=n), n) for _, d, n in stream]
+    work = sum(m.nelems * m.problem.nrhs * n for m, n in reqs)
+    with Server(max_active=16, chunk_steps=256, device=local) as srv:
+        ids = [srv.submit(m, n) for m, n in reqs]
+        res = srv.wait_all(len(ids))
+    ok = [r for r in res if r["status"] == 0]
+    makespan = max(r["t_done"] for r in ok) - min(r["t_submit"] for r in ok) if ok else None
+    lat = sorted(r["t_done"] - r["t_submit"] for r in ok)
+    t64 = 0.0
+    for m, n in reqs:
+        with Solver(m, device=local) as s:
+            s.init_explicit()
+            s.run(3)
+            s.sync()
+            ms = C.c_double(0)
+            if s.lib.exfem_gpu_run_timed(s.h, 10, C.byref(ms)) != 0:
+                return {"error": "fp64 timing failed"}
+        t64 += n * ms.value / 10.0 / 1000.0
+    served = work / makespan if makespan else None
+    sizes = [m.nelems for m, _ in reqs]
+    return {"requests": len(reqs), "ok": len(ok), "work": work, "makespan_s": makespan,
+            "served_throughput": served, "fp64_throughput": work / t64, "unit": "elem-steps*rhs/s",
+            "ratio_served_fp32_over_fp64": (served / (work / t64)) if served else None,
+            "p50_s": lat[len(lat) // 2] if lat else None, "p99_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
+            "elements_min": min(sizes), "elements_max": max(sizes),
+            "note": "burst of %d requests submitted at once (meshed beforehand), 1000-2000 steps, 1-16 angles; "
+                    "fp64 = plain FP64 GPU form, per-request ms/step x steps" % len(reqs)}
+
+
 def run_reference(args, ws, rank, dist):
     if rank != 0:
         return
@@ -359,6 +402,8 @@ def run_ours(args, ws, rank, local, dist, torch):
         del mf
 
     serving = serving_leg(args, local) if args.serve_requests > 0 else None
+    if serving is not None and args.serve_burst > 0:
+        serving["saturated"] = saturated_serving_leg(args, local)
 
     if rank != 0:
         return
@@ -393,6 +438,7 @@ def main():
     ap.add_argument("--variant", type=int, default=-1, help="force the kernel variant (FP32: 0 direct gather, 1 shared-memory tiles, 2 bulk-copy "
                          "pipeline; FP64: 0 reference order, 1 closed form)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
+    ap.add_argument("--serve-burst", type=int, default=16, help="requests in the saturated serving sample (0: skip)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     args = ap.parse_args()
     if args.warmup < 3:
