@@ -116,11 +116,26 @@ struct Ctx {
     int block_threads = 128;
     int rhs_per_thread = 1;
     bool idx32 = true;   // k_step32 with 32-bit indices (every index below 2^32)
+    int num_sms = 1;     // SMs of the context's device
     std::string err;
     // per-launch event marks while exfem_gpu_profile_kernels runs
     bool prof_on = false;
     std::vector<std::pair<const char *, cudaEvent_t>> marks;
 };
+
+// Work items per block for the free-field kernels (DRM forces, receivers).
+// Their cost is FP64 arithmetic (travel times, Ricker pulses), and an SM's
+// FP64 pipe is narrow: the same lanes spread over every SM, a few per SM,
+// finish sooner than full warps packed on a few SMs.  At most `cap` items per
+// block (the block's threads / lanes per item).
+inline int spread_per_block(long long items, int nsm, int cap) {
+    const long long per = (items + (nsm > 0 ? nsm : 1) - 1) / (nsm > 0 ? nsm : 1);
+    return (int)(per < 1 ? 1 : (per > cap ? cap : per));
+}
+inline int spread_blocks(long long items, int per_block) {
+    const long long b = (items + per_block - 1) / per_block;
+    return (int)(b < 1 ? 1 : b);
+}
 
 // Records a profiling mark after a launch (no-op unless profiling).
 void mark(Ctx &c, const char *kernel);

@@ -158,22 +158,25 @@ __device__ __forceinline__ unsigned short f2bf(float f) { return __bfloat16_as_u
 
 __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
 
-// DRM forces (model.f90:745-800) for the FP32 form: travel times in FP64,
-// the Ricker terms and the boundary/exterior split in FP32.
-__global__ void k_drm32(DevModel m) {
-    // four threads per (boundary element, rhs): thread k evaluates the free
-    // field at corner k, the quad shares the values, thread k stores forces
-    // 2k and 2k+1 (launch: 4 * ns * R threads, blocks of a multiple of 4)
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long w = t >> 2;
-    const int k = (int)(t & 3);
-    const bool valid = w < (long long)m.ns * m.R;
+// DRM forces (model.f90:745-800) of step `step` for the FP32 form: travel
+// times in FP64, the Ricker terms and the boundary/exterior split in FP32.
+// They depend on time only, so the hanging/receiver pass of step k computes
+// those of step k + 1 in extra blocks of its own launch (and the step-0 sample
+// those of step 1).  Four threads per (boundary element, rhs): thread k
+// evaluates the free field at corner k, the quad shares the values, thread k
+// stores forces 2k and 2k+1; block `b` holds items [b * ipb, (b + 1) * ipb)
+// (ipb <= threads / 4, threads a multiple of 32).  Every thread of the block
+// must call it (warp shuffles).
+__device__ __forceinline__ void drm32_items(const DevModel &m, int ipb, long long b, int step) {
+    const int li = threadIdx.x >> 2;
+    const long long w = b * ipb + li;
+    const int k = (int)(threadIdx.x & 3);
+    const bool valid = li < ipb && w < (long long)m.ns * m.R;
     int s = 0, r = 0, ie = 0;
     float uk[2] = {0.f, 0.f}, ak[2] = {0.f, 0.f};
     if (valid) {
         s = (int)(w / m.R);
         r = (int)(w % m.R);
-        int step = read_step(m) + 1;
         const DevWave &wv = m.waves[r];
         double outt = (double)step * m.dt - wv.t0;
         ie = m.s_elem[s];
@@ -879,13 +882,20 @@ __device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, con
     }
 }
 
-// Hanging nodes (anchor averages of u_hi, comp and D) and receivers.
+// Hanging nodes (anchor averages of u_hi, comp and D), receivers, and the
+// DRM forces of the next step.  Blocks [0, nb_hang) hanging nodes, then
+// nb_recv receiver blocks (ipb items each), then the DRM blocks (ipb_drm
+// items each).  mode 1: the step-0 receiver sample and the DRM forces of
+// step 1.
 __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restrict__ uho, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
-                                                unsigned short *__restrict__ dc, int nb_hang, int mode) {
+                                                unsigned short *__restrict__ dc, int nb_hang, int mode, int ipb,
+                                                int nb_recv, int ipb_drm) {
     int step = (mode == 1) ? 0 : read_step(m) + 1;
     const size_t R = m.R;
-    if ((int)blockIdx.x < nb_hang) {
+    if ((int)blockIdx.x >= nb_hang + nb_recv) {
+        drm32_items(m, ipb_drm, (long long)blockIdx.x - nb_hang - nb_recv, step + 1);
+    } else if ((int)blockIdx.x < nb_hang) {
         long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
         if (mode == 0 && t < (long long)m.n_hang * m.R) {
             int i = (int)(t / m.R), r = (int)(t % m.R);
@@ -914,11 +924,11 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
     } else if (step % m.io == 0) {
         // four threads per (receiver, rhs): thread q < 3 evaluates free-field
         // term q (the FP64 Ricker pulses are the cost), thread 0 interpolates
-        // and adds the terms in planewave_u's order
-        const long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
-        const long long wq = t >> 2;
-        const int q = (int)(t & 3);
-        const bool valid = wq < (long long)m.nrecv * m.R;
+        // and adds the terms in planewave_u's order; `ipb` items per block
+        const int li = threadIdx.x >> 2;
+        const long long wq = (long long)(blockIdx.x - nb_hang) * ipb + li;
+        const int q = (int)(threadIdx.x & 3);
+        const bool valid = li < ipb && wq < (long long)m.nrecv * m.R;
         const int slot = step / m.io;
         int i = 0, r = 0;
         bool soil = false;
@@ -1007,8 +1017,11 @@ static int pick_rpt(const Ctx &c) {
     int R = c.plan.R;
     int want = c.opts.rhs_per_thread;
     if (want == 1 || want == 2 || want == 4) return (R % want == 0) ? want : 1;
+    // measured on canyons and valleys of 3e4-9e5 elements: two per thread
+    // beats one from R = 4 (the per-term metadata and fold are shared), four
+    // pays off from R = 32
     if (R % 4 == 0 && R >= 32) return 4;
-    if (R % 2 == 0 && R >= 16) return 2;
+    if (R % 2 == 0 && R >= 4) return 2;
     return 1;
 }
 
@@ -1221,11 +1234,8 @@ int f32_init(Ctx &c) {
 int f32_launch_step(Ctx &c, int par) {
     DevModel &m = c.dm;
     float *uh = c.uhi[par], *uhn = c.uhi[par ^ 1];
-    if (m.ns > 0) {
-        k_drm32<<<nblocks(4LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
-        c.launches++;
-        mark(c, "k_drm32");
-    }
+    // (this step's DRM forces came from the previous step's k_hang32, or for
+    // step 1 from the step-0 sample)
     const int T = c.block_threads;
     const int rpt = c.rhs_per_thread;
     long long work = (long long)m.n_active * (m.R / rpt);
@@ -1279,8 +1289,13 @@ int f32_launch_step(Ctx &c, int par) {
     }
     const int TH = 256;
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + TH - 1) / TH);
-    int nbr = (int)((4LL * m.nrecv * m.R + TH - 1) / TH);   // four threads per receiver
-    k_hang32<<<nbh + nbr, TH, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0);
+    const long long WR = (long long)m.nrecv * m.R;   // four threads per (receiver, rhs)
+    const int ipb = spread_per_block(WR, c.num_sms, TH / 4);
+    const int nbr = WR > 0 ? spread_blocks(WR, ipb) : 0;
+    const long long WD = (long long)m.ns * m.R;      // four threads per (DRM element, rhs)
+    const int ipd = spread_per_block(WD, c.num_sms, TH / 4);
+    const int nbd = WD > 0 ? spread_blocks(WD, ipd) : 0;
+    k_hang32<<<nbh + nbr + nbd, TH, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0, ipb, nbr, ipd);
     c.launches++;
     mark(c, "k_hang32");
     CK(cudaGetLastError());
@@ -1290,9 +1305,15 @@ int f32_launch_step(Ctx &c, int par) {
 int f32_launch_sample0(Ctx &c, int par) {
     DevModel &m = c.dm;
     const int TH = 256;
-    int nbr = (int)((4LL * m.nrecv * m.R + TH - 1) / TH);   // four threads per receiver
-    if (nbr > 0) {
-        k_hang32<<<nbr, TH, 0, c.stream>>>(m, c.uhi[par], c.uhi[par], c.ucomp, c.udel[0], c.dcomp, 0, 1);
+    const long long WR = (long long)m.nrecv * m.R;   // four threads per (receiver, rhs)
+    const int ipb = spread_per_block(WR, c.num_sms, TH / 4);
+    const int nbr = WR > 0 ? spread_blocks(WR, ipb) : 0;
+    const long long WD = (long long)m.ns * m.R;      // DRM forces of step 1
+    const int ipd = spread_per_block(WD, c.num_sms, TH / 4);
+    const int nbd = WD > 0 ? spread_blocks(WD, ipd) : 0;
+    if (nbr + nbd > 0) {
+        k_hang32<<<nbr + nbd, TH, 0, c.stream>>>(m, c.uhi[par], c.uhi[par], c.ucomp, c.udel[0], c.dcomp, 0, 1, ipb,
+                                                  nbr, ipd);
         c.launches++;
     }
     CK(cudaGetLastError());

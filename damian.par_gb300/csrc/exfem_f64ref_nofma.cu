@@ -67,13 +67,15 @@ __device__ __forceinline__ double sqm(int i, int j) {
 // thread the corner values, summed term by term in planewave's order, and
 // thread o < 8 forms row o of both multdrm products.  For each row it applies
 // exactly the updates of the reference's loop over (i, j), in the same order,
-// so every force is bit for bit the one-thread result.  Launch: 16 * ns * R
-// threads, blocks of a multiple of 16.
-__global__ void k_drm_ref(DevModel m) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long w = t >> 4;
-    const int l = (int)(t & 15), corner = l >> 2, term = l & 3;
-    const bool valid = w < (long long)m.ns * m.R;
+// so every force is bit for bit the one-thread result.  Block `b` holds items
+// [b * ipb, (b + 1) * ipb) (ipb <= threads / 16, threads a multiple of 32);
+// every thread of the block must call it (warp shuffles).  The forces depend
+// on time only: `step` is the step they are for.
+__device__ __forceinline__ void drm_ref_items(const DevModel &m, int ipb, long long b, int step) {
+    const int li = threadIdx.x >> 4;
+    const long long w = b * ipb + li;
+    const int l = (int)(threadIdx.x & 15), corner = l >> 2, term = l & 3;
+    const bool valid = li < ipb && w < (long long)m.ns * m.R;
     int s = 0, r = 0, ie = 0;
     double p0x = 0.0, p0z = 0.0, p2x = 0.0, p2z = 0.0;   // columns u and ddu of this term
     if (valid) {
@@ -81,7 +83,6 @@ __global__ void k_drm_ref(DevModel m) {
         r = (int)(w % m.R);
         ie = m.s_elem[s];
         if (term < 3) {
-            int step = *(volatile int *)m.d_step + 1;
             const DevWave wv = m.waves[r];
             double outt = (double)step * m.dt - wv.t0;
             int x = m.econn[4 * ie + corner];
@@ -128,6 +129,12 @@ __global__ void k_drm_ref(DevModel m) {
             }
     m.fdrm[((size_t)s * 16 + o) * m.R + r] = pk;
     m.fdrm[((size_t)s * 16 + 8 + o) * m.R + r] = pm * m.emass[ie];
+}
+
+// DRM forces of the current step (read from the device step counter), on
+// their own: the step without allocation, whose counters are its own.
+__global__ void k_drm_ref(DevModel m, int ipb) {
+    drm_ref_items(m, ipb, blockIdx.x, *(volatile int *)m.d_step + 1);
 }
 
 __global__ void __launch_bounds__(128) k_elem_ref(DevModel m, const double *__restrict__ u,
@@ -240,10 +247,19 @@ __device__ __forceinline__ void load_u64(const DevModel &m, const double *u, int
 // Hanging nodes (set_dispshanging) and receiver samples (visu_field,
 // visualization.f90:156-181): blocks [0, nb_hang) do the hanging nodes, the
 // rest sample the receivers on save steps.  mode 1 records the step-0 sample.
-__global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict__ unew, int nb_hang, int mode) {
+// Hanging nodes, receivers, and (reference-order variant) the DRM forces of
+// the next step, which depend on time only: blocks [0, nb_hang) hanging
+// nodes, then nb_recv receiver blocks (ipb items each), then the DRM blocks
+// (ipb_drm items each).  mode 1: the step-0 receiver sample and the DRM
+// forces of step 1.  (In the element kernel's launch instead, the DRM blocks
+// slowed the elements by what they saved here: both wait on the FP64 pipe.)
+__global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict__ unew, int nb_hang, int mode, int ipb,
+                                                  int nb_recv, int ipb_drm) {
     int step = (mode == 1) ? 0 : *(volatile int *)m.d_step + 1;
     const size_t R = m.R;
-    if ((int)blockIdx.x < nb_hang) {
+    if ((int)blockIdx.x >= nb_hang + nb_recv) {
+        drm_ref_items(m, ipb_drm, (long long)blockIdx.x - nb_hang - nb_recv, step + 1);
+    } else if ((int)blockIdx.x < nb_hang) {
         long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
         if (mode == 0 && t < (long long)m.n_hang * m.R) {
             int i = (int)(t / m.R), r = (int)(t % m.R);
@@ -254,11 +270,11 @@ __global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict
     } else if (step % m.io == 0) {
         // four threads per (receiver, rhs): thread q < 3 evaluates free-field
         // term q (the FP64 Ricker pulses are the cost), thread 0 interpolates
-        // and adds the terms in planewave_u's order
-        const long long t = (long long)(blockIdx.x - nb_hang) * blockDim.x + threadIdx.x;
-        const long long wq = t >> 2;
-        const int q = (int)(t & 3);
-        const bool valid = wq < (long long)m.nrecv * m.R;
+        // and adds the terms in planewave_u's order; `ipb` items per block
+        const int li = threadIdx.x >> 2;
+        const long long wq = (long long)(blockIdx.x - nb_hang) * ipb + li;
+        const int q = (int)(threadIdx.x & 3);
+        const bool valid = li < ipb && wq < (long long)m.nrecv * m.R;
         const int slot = step / m.io;
         int i = 0, r = 0;
         bool soil = false;
@@ -321,11 +337,8 @@ int f64ref_launch_drm_elem_node(Ctx &c, int par) {
     DevModel &m = c.dm;
     double *u = c.u64[par], *um = c.u64[par ^ 1];
     const int T = 128;
-    if (m.ns > 0) {
-        k_drm_ref<<<nblocks(16LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
-        c.launches++;
-        mark(c, "k_drm_ref");
-    }
+    // (this step's DRM forces came from the previous step's k_hang_ref, or
+    // for step 1 from the step-0 sample)
     k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, u, um, c.ef64);
     mark(c, "k_elem_ref");
     k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, c.ef64, um);
@@ -334,14 +347,21 @@ int f64ref_launch_drm_elem_node(Ctx &c, int par) {
     return cudaGetLastError() == cudaSuccess ? EXFEM_OK : EXFEM_E_CUDA;
 }
 
-// Hanging + receivers for both FP64 variants; mode 1 = step-0 sample.
+// Hanging + receivers for both FP64 variants, plus the next step's DRM forces
+// for the reference-order one; mode 1 = step-0 sample (and step 1's forces).
 int f64_launch_hang(Ctx &c, double *unew, int mode) {
     DevModel &m = c.dm;
     const int T = 128;
     int nbh = mode == 1 ? 0 : (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);
-    int nbr = (int)((4LL * m.nrecv * m.R + T - 1) / T);   // four threads per receiver
-    if (nbh + nbr == 0) return EXFEM_OK;
-    k_hang_ref<<<nbh + nbr, T, 0, c.stream>>>(m, unew, nbh, mode);
+    const long long WR = (long long)m.nrecv * m.R;   // four threads per (receiver, rhs)
+    const int ipb = spread_per_block(WR, c.num_sms, T / 4);
+    const int nbr = WR > 0 ? spread_blocks(WR, ipb) : 0;
+    const bool drm = c.opts.variant == EXFEM_VARIANT_REFERENCE_ORDER && m.ns > 0;
+    const long long WD = drm ? (long long)m.ns * m.R : 0;   // sixteen threads per (DRM element, rhs)
+    const int ipd = spread_per_block(WD, c.num_sms, T / 16);
+    const int nbd = WD > 0 ? spread_blocks(WD, ipd) : 0;
+    if (nbh + nbr + nbd == 0) return EXFEM_OK;
+    k_hang_ref<<<nbh + nbr + nbd, T, 0, c.stream>>>(m, unew, nbh, mode, ipb, nbr, ipd);
     c.launches++;
     mark(c, "k_hang_ref");
     return cudaGetLastError() == cudaSuccess ? EXFEM_OK : EXFEM_E_CUDA;
@@ -427,11 +447,15 @@ extern "C" int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_
     double *ef = base + ef_off;
     const int T = 128;
     k_noalloc_prep<<<1, 1, 0, c.stream>>>(counters, step);
-    if (m.ns > 0) k_drm_ref<<<nblocks(16LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
+    if (m.ns > 0) {
+        const long long W = (long long)m.ns * m.R;
+        const int ipb = spread_per_block(W, c.num_sms, 8);
+        k_drm_ref<<<spread_blocks(W, ipb), 128, 0, c.stream>>>(m, ipb);
+    }
     k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, d_u, d_um, ef);
     k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, ef, d_unew);
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);
-    k_hang_ref<<<nbh, T, 0, c.stream>>>(m, d_unew, nbh, 0);
+    k_hang_ref<<<nbh, T, 0, c.stream>>>(m, d_unew, nbh, 0, 1, 0, 1);
     e = cudaGetLastError();
     if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
     c.launches += 4 + (m.ns > 0 ? 1 : 0);

@@ -51,12 +51,12 @@ __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile 
 // the consistent mass (model.f90:766-798), in closed form.  Four threads per
 // (boundary element, rhs): thread k evaluates the free field at corner k, the
 // quad shares the values by shuffles, thread k stores forces 2k and 2k+1
-// (launch: 4 * ns * R threads, blocks of a multiple of 4).
-__global__ void k_drm(DevModel m) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long w = t >> 2;
-    const int k = (int)(t & 3);
-    const bool valid = w < (long long)m.ns * m.R;
+// (launch: `ipb` items per block of 4 * ipb or more threads, a multiple of 32).
+__global__ void k_drm(DevModel m, int ipb) {
+    const int li = threadIdx.x >> 2;
+    const long long w = (long long)blockIdx.x * ipb + li;
+    const int k = (int)(threadIdx.x & 3);
+    const bool valid = li < ipb && w < (long long)m.ns * m.R;
     int s = 0, r = 0, ie = 0;
     double ukx = 0.0, ukz = 0.0, akx = 0.0, akz = 0.0;
     if (valid) {
@@ -255,7 +255,9 @@ int launch_step64(Ctx &c, int par) {
     } else {
         const int T = c.block_threads;
         if (m.ns > 0) {
-            k_drm<<<nblocks(4LL * m.ns * m.R, 128), 128, 0, c.stream>>>(m);
+            const long long W = (long long)m.ns * m.R;
+            const int ipb = spread_per_block(W, c.num_sms, 32);
+            k_drm<<<spread_blocks(W, ipb), 128, 0, c.stream>>>(m, ipb);
             c.launches++;
             mark(c, "k_drm");
         }
@@ -425,14 +427,18 @@ int capture_graph(Ctx &c, int g) {
 }
 
 int launches_per_step(const Ctx &c) {
-    if (c.precision == EXFEM_FP64) return (c.dm.ns > 0 ? 1 : 0) + 3;   // drm, elem, node, hang
-    return (c.dm.ns > 0 ? 1 : 0) + 2;
+    // the reference-order FP64 variant and the FP32 form compute the next
+    // step's DRM forces inside their hanging/receiver kernel
+    if (c.precision == EXFEM_FP64)
+        return (c.dm.ns > 0 && c.opts.variant != EXFEM_VARIANT_REFERENCE_ORDER ? 1 : 0) + 3;   // (drm,) elem, node, hang
+    return 2 + (c.p32_n > 0 ? 1 : 0);   // step, (point,) hang
 }
 
 // Device side of exfem_gpu_create: stream, uploads, state buffers.
 int create_device(Ctx &c, const exfem_mesh &mesh) {
     CK(cudaSetDevice(c.device));
     CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    CK(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, c.device));
     // node coordinates in internal order (free field at DRM corners)
     TRY(upload(c, c.plan.nxy, &c.dm.nxy));   // internal node coordinates
     TRY(setup_device(c));
