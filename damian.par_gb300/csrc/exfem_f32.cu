@@ -904,20 +904,38 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
             // the one hanging value that is not its anchors' average, so at
             // the first step the increment of such a node is new - old.
             const bool from_row = m.point_kind == EXFEM_POINT_DISP && step == 1 && m.pflag[h];
+            // every input of both dofs is loaded before the first store (the
+            // stores could alias the anchors' rows for all the compiler knows,
+            // which would serialise the two dofs' round trips)
+            size_t ih[2], ia[2], ib[2];
+            float ua[2], ub[2], da[2], db[2];
+            unsigned short uca[2], ucb[2], dca[2], dcb[2];
+            double u_old[2];
 #pragma unroll
             for (int d = 0; d < 2; ++d) {
-                size_t ih = ((size_t)h * 2 + d) * R + r, ia = ((size_t)a * 2 + d) * R + r,
-                       ib = ((size_t)b * 2 + d) * R + r;
-                const double u_old = (double)uho[ih] - (double)bf2f(uc[ih]);   // the row before this step
-                uhn[ih] = 0.5f * (uhn[ia] + uhn[ib]);
-                uc[ih] = f2bf(0.5f * (bf2f(uc[ia]) + bf2f(uc[ib])));
+                ih[d] = ((size_t)h * 2 + d) * R + r;
+                ia[d] = ((size_t)a * 2 + d) * R + r;
+                ib[d] = ((size_t)b * 2 + d) * R + r;
+                u_old[d] = (double)uho[ih[d]] - (double)bf2f(uc[ih[d]]);   // the row before this step
+                ua[d] = uhn[ia[d]]; ub[d] = uhn[ib[d]];
+                uca[d] = uc[ia[d]]; ucb[d] = uc[ib[d]];
+                da[d] = dh[ia[d]]; db[d] = dh[ib[d]];
+                dca[d] = dc[ia[d]]; dcb[d] = dc[ib[d]];
+            }
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const float un = 0.5f * (ua[d] + ub[d]);
+                const unsigned short ucn = f2bf(0.5f * (bf2f(uca[d]) + bf2f(ucb[d])));
+                uhn[ih[d]] = un;
+                uc[ih[d]] = ucn;
                 if (from_row) {
-                    const double dn = ((double)uhn[ih] - (double)bf2f(uc[ih])) - u_old;
-                    dh[ih] = (float)dn;
-                    dc[ih] = f2bf((float)((double)dh[ih] - dn));
+                    const double dn = ((double)un - (double)bf2f(ucn)) - u_old[d];
+                    const float dnf = (float)dn;
+                    dh[ih[d]] = dnf;
+                    dc[ih[d]] = f2bf((float)((double)dnf - dn));
                 } else {
-                    dh[ih] = 0.5f * (dh[ia] + dh[ib]);
-                    dc[ih] = f2bf(0.5f * (bf2f(dc[ia]) + bf2f(dc[ib])));
+                    dh[ih[d]] = 0.5f * (da[d] + db[d]);
+                    dc[ih[d]] = f2bf(0.5f * (bf2f(dca[d]) + bf2f(dcb[d])));
                 }
             }
         }
