@@ -254,9 +254,17 @@ def saturated_serving_leg(args, local):
         t64 += n * ms.value / 10.0 / 1000.0
     served = work / makespan if makespan else None
     sizes = [m.nelems for m, _ in reqs]
+    # algorithmic HBM bytes of the served steps (the FP32 step kernel's and the
+    # hanging/receiver pass's, as in the roofline) over the makespan
+    abytes = sum(n * ((kernel_bytes("k_step32", m, m.problem.nrhs, False) or 0) +
+                      (kernel_bytes("k_hang32", m, m.problem.nrhs, False) or 0)) for m, n in reqs)
+    peak, peak_kind = measured_peaks()
+    served_gbs = abytes / makespan / 1e9 if makespan else None
     return {"requests": len(reqs), "ok": len(ok), "work": work, "makespan_s": makespan,
             "served_throughput": served, "fp64_throughput": work / t64, "unit": "elem-steps*rhs/s",
             "ratio_served_fp32_over_fp64": (served / (work / t64)) if served else None,
+            "served_algorithmic_gbs": served_gbs,
+            "served_hbm_frac": (served_gbs / peak) if (served_gbs and peak) else None, "peak_kind": peak_kind,
             "p50_s": lat[len(lat) // 2] if lat else None, "p99_s": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
             "elements_min": min(sizes), "elements_max": max(sizes),
             "note": "burst of %d requests submitted at once (meshed beforehand), 1000-2000 steps, 1-16 angles; "
