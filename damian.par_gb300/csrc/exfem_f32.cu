@@ -17,13 +17,15 @@
 // anchor average after every step and a prescribed displacement at t = 0).  Templates, masses, dashpots, hanging
 // weights and dt stay FP64 on the host and are rounded once.
 //
-// One step is three kernels:
-//   k_drm32    DRM effective forces in FP64, stored FP32
+// One step is two kernels (three with a point source):
 //   k_step32   per (non-hanging node, group of right-hand sides): gather the
 //              closed-form Q4 forces of its elements from u_hi, the DRM terms,
 //              the dashpot and anchor terms, update D and u (fused; no
 //              element buffer)
-//   k_hang32   hanging nodes = anchor averages; receivers in FP64
+//   k_point32  (point sources) the source term at its nodes
+//   k_hang32   hanging nodes = anchor averages; receivers in FP64; and the
+//              next step's DRM effective forces (travel times FP64, stored
+//              FP32), which depend on time only
 // State layout: value (node n, dof d, rhs r) at (n*2 + d)*R + r, so a warp
 // reads R contiguous values per (node, dof) and one set of mesh metadata
 // serves every right-hand side.
