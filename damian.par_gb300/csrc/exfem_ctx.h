@@ -149,7 +149,6 @@ int f32_alloc(Ctx &c);
 int f32_init(Ctx &c);
 int f32_launch_step(Ctx &c, int par);
 int f32_launch_sample0(Ctx &c, int par);
-int f32_get_u(Ctx &c, int rhs, std::vector<double> &out_internal);
 // bf16 <-> float on the host (round to nearest even), for tests and read-back.
 float bf16_to_float(unsigned short h);
 

@@ -1340,23 +1340,6 @@ int f32_launch_sample0(Ctx &c, int par) {
     return EXFEM_OK;
 }
 
-int f32_get_u(Ctx &c, int rhs, std::vector<double> &out) {
-    const Plan &P = c.plan;
-    size_t nst = (size_t)P.nn * 2 * P.R;
-    std::vector<float> hi(nst);
-    std::vector<unsigned short> co(nst);
-    CK(cudaMemcpy(hi.data(), c.uhi[c.parity], nst * sizeof(float), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(co.data(), c.ucomp, nst * sizeof(unsigned short), cudaMemcpyDeviceToHost));
-    c.d2h_bytes += nst * (sizeof(float) + sizeof(unsigned short));
-    out.resize((size_t)P.nn * 2);
-    for (int i = 0; i < P.nn; ++i)
-        for (int d = 0; d < 2; ++d) {
-            size_t k = ((size_t)i * 2 + d) * P.R + rhs;
-            out[2 * (size_t)i + d] = (double)hi[k] - (double)bf16_to_float(co[k]);
-        }
-    return EXFEM_OK;
-}
-
 float bf16_to_float(unsigned short h) {
     unsigned w = (unsigned)h << 16;
     float f;

@@ -247,6 +247,17 @@ __global__ void k_sample_points(DevModel m, const double *__restrict__ u64, cons
     out[2 * (size_t)i + 1] = fy;
 }
 
+// One right-hand side of the state in internal dof order (2 per node): the
+// FP64 value, or u_hi - u_comp in FP64 for the FP32 form.
+__global__ void k_extract_rhs(const double *__restrict__ u64, const float *__restrict__ uh,
+                              const unsigned short *__restrict__ uc, int R, int rhs, long long ndof,
+                              double *__restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ndof) return;
+    const size_t k = (size_t)i * R + rhs;
+    out[i] = u64 ? u64[k] : (double)uh[k] - (double)__bfloat162float(__ushort_as_bfloat16(uc[k]));
+}
+
 int launch_step64(Ctx &c, int par) {
     DevModel &m = c.dm;
     double *u = c.u64[par], *um = c.u64[par ^ 1];
@@ -635,19 +646,23 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     const Plan &P = c.plan;
     if (rhs < 0 || rhs >= P.R || n < (size_t)2 * P.nn) { c.err = "bad rhs or buffer too small"; return EXFEM_E_ARG; }
     CK(cudaSetDevice(c.device));
-    CK(cudaStreamSynchronize(c.stream));
-    std::vector<double> in;
-    if (c.precision == EXFEM_FP64) {
-        std::vector<double> all((size_t)P.nn * 2 * P.R);
-        CK(cudaMemcpy(all.data(), c.u64[c.parity], all.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        c.d2h_bytes += all.size() * sizeof(double);
-        in.resize((size_t)P.nn * 2);
-        for (int i = 0; i < P.nn; ++i)
-            for (int d = 0; d < 2; ++d) in[2 * (size_t)i + d] = all[((size_t)i * 2 + d) * P.R + rhs];
-    } else {
-        int rc = f32_get_u(c, rhs, in);
-        if (rc) return rc;
-    }
+    // the right-hand side is gathered on the device, so only its 2 * nn
+    // values cross to the host (not the whole batched state)
+    const long long ndof = 2LL * P.nn;
+    std::vector<double> in((size_t)ndof);
+    double *d = nullptr;
+    CK(cudaMalloc(&d, (size_t)ndof * sizeof(double)));
+    const bool f64 = c.precision == EXFEM_FP64;
+    k_extract_rhs<<<nblocks(ndof, 256), 256, 0, c.stream>>>(f64 ? c.u64[c.parity] : nullptr,
+                                                            f64 ? nullptr : c.uhi[c.parity], c.ucomp, P.R, rhs,
+                                                            ndof, d);
+    c.launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(in.data(), d, (size_t)ndof * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    cudaFree(d);
+    if (e != cudaSuccess) { c.err = std::string("get_u: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    c.d2h_bytes += (size_t)ndof * sizeof(double);
     for (int i = 0; i < P.nn; ++i) {
         int rn = P.ref_of_node[i];
         u[2 * (size_t)rn] = in[2 * (size_t)i];

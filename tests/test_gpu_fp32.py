@@ -121,6 +121,25 @@ def test_tiled_and_direct_kernels_agree():
         assert np.array_equal(ua[r], ub[r]), r
 
 
+def test_get_u_copies_one_rhs():
+    """exfem_gpu_get_u gathers the requested right-hand side on the device:
+    2 * nnodes doubles cross to the host, not the batched state (FP32 and
+    FP64 contexts)."""
+    m = workloads.build("valley_batched", scale=0.08, steps=20)
+    assert m.problem.nrhs == 64
+    for prec in (EXFEM_FP32_KAHAN, 0):
+        with Solver(m, precision=prec) as s:
+            s.init_explicit()
+            s.run(6)
+            s.sync()
+            _, d0 = s.copy_bytes()
+            u = s.u(37)
+            _, d1 = s.copy_bytes()
+            assert u.size == 2 * m.nnodes
+            assert d1 - d0 == 2 * m.nnodes * 8
+            assert np.isfinite(u).all()
+
+
 @pytest.mark.parametrize("rpt", [4, 2, 1])
 def test_32_and_64_bit_indices_agree(rpt):
     """k_step32's 32-bit index form (shift and mask thread split) and its
