@@ -31,7 +31,7 @@ struct DevModel {
     const int *econn;        // 4 per element
     const double *ecoef;     // 4 per element (FP64)
     const float *ecoef32;    // 4 per element (FP32)
-    const double *emulam;    // 2 per element: (mu, lambda)
+    const double *ekv;       // 6 per element: calck_values(mu, lambda)
     const double *emass;     // per element
     const int *edamp;        // per element, -1 or slot
     const double *edampv;    // 8 per slot

@@ -51,6 +51,26 @@ __host__ __device__ __forceinline__ void q4_ku_corner(T A, T B, T C, T D, const 
     fy = sP * S + sQ * F2 + sG * Gy;
 }
 
+// calck (formulation.f90:276-313), column-major k[col*8+row].  Its 64 entries
+// are six values with signs, kv = (3m+l)/3, (m+l)/4, (3m+2l)/6, (m-l)/4,
+// (3m+l)/6, l/6 (calck_values, exfem_plan.h), computed once per element on
+// the host with the formula's operations, as the reference computes m_kmat
+// once per material (explicit.f90:139).  Negation is exact, so every entry
+// is the formula's own rounding.
+__host__ __device__ __forceinline__ void calck(const double kv[6], double k[64]) {
+    const double v[64] = {
+        kv[0], kv[1], -kv[2], -kv[3], -kv[4], -kv[1], kv[5], kv[3],
+        kv[1], kv[0], kv[3], kv[5], -kv[1], -kv[4], -kv[3], -kv[2],
+        -kv[2], kv[3], kv[0], -kv[1], kv[5], -kv[3], -kv[4], kv[1],
+        -kv[3], kv[5], -kv[1], kv[0], kv[3], -kv[2], kv[1], -kv[4],
+        -kv[4], -kv[1], kv[5], kv[3], kv[0], kv[1], -kv[2], -kv[3],
+        -kv[1], -kv[4], -kv[3], -kv[2], kv[1], kv[0], kv[3], kv[5],
+        kv[5], -kv[3], -kv[4], kv[1], -kv[2], kv[3], kv[0], -kv[1],
+        kv[3], -kv[2], kv[1], -kv[4], -kv[3], kv[5], -kv[1], kv[0]};
+#pragma unroll
+    for (int i = 0; i < 64; ++i) k[i] = v[i];
+}
+
 __host__ __device__ __forceinline__ float q4fma(float a, float b, float c) { return fmaf(a, b, c); }
 __host__ __device__ __forceinline__ double q4fma(double a, double b, double c) { return fma(a, b, c); }
 

@@ -26,28 +26,7 @@ namespace exfem {
 
 namespace {
 
-// calck (formulation.f90:276-313), column-major k[col*8+row].
-__device__ __forceinline__ void calck(double m, double l, double k[64]) {
-    const double v[64] = {
-        (3.0 * m + l) / 3.0, (m + l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, -(m - l) / 4.0,
-        -(3.0 * m + l) / 6.0, -(m + l) / 4.0, l / 6.0, (m - l) / 4.0,
-        (m + l) / 4.0, (3.0 * m + l) / 3.0, (m - l) / 4.0, l / 6.0,
-        -(m + l) / 4.0, -(3.0 * m + l) / 6.0, -(m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0,
-        -(3.0 * m + 2.0 * l) / 6.0, (m - l) / 4.0, (3.0 * m + l) / 3.0, -(m + l) / 4.0,
-        l / 6.0, -(m - l) / 4.0, -(3.0 * m + l) / 6.0, (m + l) / 4.0,
-        -(m - l) / 4.0, l / 6.0, -(m + l) / 4.0, (3.0 * m + l) / 3.0,
-        (m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, (m + l) / 4.0, -(3.0 * m + l) / 6.0,
-        -(3.0 * m + l) / 6.0, -(m + l) / 4.0, l / 6.0, (m - l) / 4.0,
-        (3.0 * m + l) / 3.0, (m + l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, -(m - l) / 4.0,
-        -(m + l) / 4.0, -(3.0 * m + l) / 6.0, -(m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0,
-        (m + l) / 4.0, (3.0 * m + l) / 3.0, (m - l) / 4.0, l / 6.0,
-        l / 6.0, -(m - l) / 4.0, -(3.0 * m + l) / 6.0, (m + l) / 4.0,
-        -(3.0 * m + 2.0 * l) / 6.0, (m - l) / 4.0, (3.0 * m + l) / 3.0, -(m + l) / 4.0,
-        (m - l) / 4.0, -(3.0 * m + 2.0 * l) / 6.0, (m + l) / 4.0, -(3.0 * m + l) / 6.0,
-        -(m - l) / 4.0, l / 6.0, -(m + l) / 4.0, (3.0 * m + l) / 3.0};
-#pragma unroll
-    for (int i = 0; i < 64; ++i) k[i] = v[i];
-}
+
 
 // calcsqm (formulation.f90:256-268) entry (i, j): same component only,
 // 4 on the diagonal, 2 for edge-adjacent corners, 1 for the opposite corner.
@@ -113,7 +92,12 @@ __device__ __forceinline__ void drm_ref_items(const DevModel &m, int ipb, long l
     const int o = l;
     unsigned e = drm_mask(m.s_kind[s]);
     double K[64];
-    calck(m.emulam[2 * ie], m.emulam[2 * ie + 1], K);
+    {
+        const double2 *kv2 = reinterpret_cast<const double2 *>(m.ekv + (size_t)ie * 6);
+        const double2 a = kv2[0], b = kv2[1], c6 = kv2[2];
+        const double kv[6] = {a.x, a.y, b.x, b.y, c6.x, c6.y};
+        calck(kv, K);
+    }
     double pk = 0.0, pm = 0.0;
     for (int i = 0; i < 8; ++i)
         for (int j = 0; j < 8; ++j)
@@ -162,9 +146,13 @@ __global__ void __launch_bounds__(128) k_elem_ref(DevModel m, const double *__re
 #pragma unroll
         for (int k = 0; k < 8; ++k) lr[k] = lr[k] + m.a2 * dv[k] * lp[k];
     }
-    double2 ml = reinterpret_cast<const double2 *>(m.emulam)[e];
     double K[64];
-    calck(ml.x, ml.y, K);
+    {
+        const double2 *kv2 = reinterpret_cast<const double2 *>(m.ekv + (size_t)e * 6);
+        const double2 a = kv2[0], b = kv2[1], c6 = kv2[2];
+        const double kv[6] = {a.x, a.y, b.x, b.y, c6.x, c6.y};
+        calck(kv, K);
+    }
 #pragma unroll
     for (int col = 0; col < 8; ++col) {
         double temp = -1.0 * lu[col];

@@ -329,11 +329,11 @@ int setup_device(Ctx &c) {
     TRY(upload(c, P.emass, &m.emass));
     // arrays only the FP64 kernels read (the FP32 step folds mass, damping
     // and the operator into its own per-node and per-term arrays)
-    m.emulam = nullptr; m.mfull = nullptr; m.ownptr = nullptr; m.ownlist = nullptr;
+    m.ekv = nullptr; m.mfull = nullptr; m.ownptr = nullptr; m.ownlist = nullptr;
     m.odptr = nullptr; m.odlist = nullptr; m.edamp = nullptr; m.edampv = nullptr;
     m.ecoef = nullptr; m.inv_mfull = nullptr;
     if (c.precision == EXFEM_FP64) {
-        TRY(upload(c, P.emulam, &m.emulam));
+        TRY(upload(c, P.ekv, &m.ekv));
         TRY(upload(c, P.mfull_int, &m.mfull));
         TRY(upload(c, P.ownptr, &m.ownptr));
         TRY(upload(c, P.ownlist, &m.ownlist));
@@ -824,7 +824,7 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
     size_t b = 16 * nn;                                            // node coordinates
     b += ne * (16 + 8);                                            // conn, mass
     if (f64) {
-        b += ne * (16 + 4 + 32 + 16);                              // (mu,l), damp slot, coef, own list
+        b += ne * (48 + 4 + 32 + 16);                              // calck values, damp slot, coef, own list
         b += 64 * std::min(ne, 4 * nabs + 4);                      // dashpot values of boundary elements
         b += 2 * 4 * (nn + 1) + 32 * nn;                           // own and DRM-own pointers, m_full, 1/m_full
     }

@@ -404,6 +404,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     P.ecoef32.resize((size_t)ne * 4);
     P.emass.resize(ne);
     P.emulam.resize((size_t)ne * 2);
+    P.ekv.resize((size_t)ne * 6);
     P.edampv.clear();
     pvec<double> eh;
     eh.resize(ne);
@@ -423,6 +424,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         eh[ie] = h;
         P.emulam[(size_t)ie * 2] = mu;
         P.emulam[(size_t)ie * 2 + 1] = lam;
+        calck_values(mu, lam, &P.ekv[(size_t)ie * 6]);
         P.ecoef[(size_t)ie * 4 + 0] = (lam + 2.0 * mu) / 4.0;
         P.ecoef[(size_t)ie * 4 + 1] = lam / 4.0;
         P.ecoef[(size_t)ie * 4 + 2] = mu / 4.0;

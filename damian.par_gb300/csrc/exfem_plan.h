@@ -52,6 +52,18 @@ struct WaveConst {
 
 int init_wave_const(const exfem_wave &w, double alpha, double beta, WaveConst &out, std::string &err);
 
+// The six distinct magnitudes of calck(mu, lambda) (formulation.f90:276-313),
+// each with the formula's operations: (3m+l)/3, (m+l)/4, (3m+2l)/6, (m-l)/4,
+// (3m+l)/6, l/6.  The FP64 kernels rebuild K from them with signs.
+inline void calck_values(double m, double l, double kv[6]) {
+    kv[0] = (3.0 * m + l) / 3.0;
+    kv[1] = (m + l) / 4.0;
+    kv[2] = (3.0 * m + 2.0 * l) / 6.0;
+    kv[3] = (m - l) / 4.0;
+    kv[4] = (3.0 * m + l) / 6.0;
+    kv[5] = l / 6.0;
+}
+
 struct Plan {
     int nn = 0, ne = 0, R = 1;
     int n_active = 0;               // non-hanging nodes are internal [0, n_active)
@@ -65,7 +77,8 @@ struct Plan {
     pvec<int> econn;                // 4 per element: internal node ids of the non-hanging corners
     pvec<double> ecoef;             // 4 per element: (lam+2mu)/4, lam/4, mu/4, (lam+3mu)/12
     pvec<float> ecoef32;            // same, FP32
-    pvec<double> emulam;            // 2 per element: (mu, lambda) for calck in reference order
+    pvec<double> emulam;            // 2 per element: (mu, lambda)
+    pvec<double> ekv;               // 6 per element: calck_values(mu, lambda)
     pvec<double> emass;             // rho*(h/2)^2 per element (getmassof)
     pvec<int> edamp;                // per element: index into edampv or -1
     std::vector<double> edampv;     // 8 per damped element (getdampingof)

@@ -19,6 +19,20 @@ def ku(mu, lam):
     return k
 
 
+def test_calck_rebuilt_from_six_values_is_bitwise():
+    """The FP64 kernels rebuild calck's 8x8 matrix from six per-element values
+    computed on the host; every entry must carry the formula's own bits, for
+    the materials of the configs and for random (mu, lambda)."""
+    L = npb.lib()
+    rng = np.random.default_rng(3)
+    cases = [(2000.0 * 1000.0 ** 2, 2000.0 * (2000.0 ** 2 - 2 * 1000.0 ** 2)),   # configs 0/1
+             (1800.0 * 300.0 ** 2, 1800.0 * (700.0 ** 2 - 2 * 300.0 ** 2)),      # valley infill
+             (1.0, -0.5), (3.0, 0.0)]
+    cases += [(float(a), float(b)) for a, b in zip(rng.uniform(1e5, 1e10, 200), rng.uniform(-5e9, 1e10, 200))]
+    for mu, lam in cases:
+        assert L.probe_calck_check(mu, lam) == -1, (mu, lam)
+
+
 def test_closed_form_q4_matches_calck():
     rng = np.random.default_rng(3)
     L = npb.lib()
