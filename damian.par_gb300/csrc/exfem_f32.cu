@@ -1039,8 +1039,8 @@ static int pick_rpt(const Ctx &c) {
     if (want == 1 || want == 2 || want == 4) return (R % want == 0) ? want : 1;
     // measured on canyons and valleys of 3e4-9e5 elements: two per thread
     // beats one from R = 4 (the per-term metadata and fold are shared), four
-    // pays off from R = 32
-    if (R % 4 == 0 && R >= 32) return 4;
+    // pays off from R = 16
+    if (R % 4 == 0 && R >= 16) return 4;
     if (R % 2 == 0 && R >= 4) return 2;
     return 1;
 }

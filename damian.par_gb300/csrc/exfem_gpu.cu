@@ -486,6 +486,7 @@ void exfem_gpu_default_opts(exfem_opts *o) {
     o->check_every = 0;
     o->variant = EXFEM_VARIANT_REFERENCE_ORDER;
     o->index_bits = 0;
+    o->pad_rhs = 0;
 }
 
 int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts, exfem_ctx **out) {
@@ -501,6 +502,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
         return EXFEM_E_ARG;
     }
     if (o.index_bits != 0 && o.index_bits != 64) { g_create_err = "index_bits must be 0 or 64"; return EXFEM_E_ARG; }
+    if (o.pad_rhs != 0 && o.pad_rhs != 1) { g_create_err = "pad_rhs must be 0 or 1"; return EXFEM_E_ARG; }
     const int max_bt = o.precision == EXFEM_FP64 ? 256 : 512;   // the kernels' __launch_bounds__
     if (o.block_threads < 0 || o.block_threads > max_bt || (o.block_threads % 32) != 0) {
         g_create_err = "block_threads must be a multiple of 32 in [0, " + std::to_string(max_bt) + "]";
@@ -518,7 +520,8 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     c->device = o.device;
     int rc;
     try {
-        rc = build_plan(*mesh, *prob, o.reorder != 0, c->plan, c->err);
+        const int r_int = (o.precision == EXFEM_FP32_KAHAN && o.pad_rhs == 0) ? padded_rhs(prob->nrhs) : 0;
+        rc = build_plan(*mesh, *prob, o.reorder != 0, c->plan, c->err, r_int);
     } catch (const std::bad_alloc &) {
         rc = EXFEM_E_NOMEM;
         c->err = "host allocation failed while preparing the model";
@@ -644,7 +647,7 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     if (!ctx || !u) return EXFEM_E_ARG;
     Ctx &c = *ctx;
     const Plan &P = c.plan;
-    if (rhs < 0 || rhs >= P.R || n < (size_t)2 * P.nn) { c.err = "bad rhs or buffer too small"; return EXFEM_E_ARG; }
+    if (rhs < 0 || rhs >= P.R_user || n < (size_t)2 * P.nn) { c.err = "bad rhs or buffer too small"; return EXFEM_E_ARG; }
     CK(cudaSetDevice(c.device));
     // the right-hand side is gathered on the device, so only its 2 * nn
     // values cross to the host (not the whole batched state)
@@ -675,7 +678,9 @@ int exfem_gpu_get_seismograms(exfem_ctx *ctx, double *out, size_t cap, int *nsav
     if (!ctx) return EXFEM_E_ARG;
     Ctx &c = *ctx;
     const Plan &P = c.plan;
-    size_t need = (size_t)P.R * P.nsave * P.nrecv * 2;
+    // right-hand side r's samples are block r (r-major): the caller's are the
+    // first R_user blocks, any padding follows them
+    size_t need = (size_t)P.R_user * P.nsave * P.nrecv * 2;
     if (nsaved) *nsaved = c.steps_done / P.io + 1;
     if (!out) return EXFEM_OK;
     if (cap < need) { c.err = "seismogram buffer too small"; return EXFEM_E_ARG; }
@@ -756,7 +761,7 @@ int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *x
     if (!ctx) return EXFEM_E_ARG;
     Ctx &c = *ctx;
     if (!c.inited) { c.err = "exfem_gpu_sample_points before exfem_gpu_init_explicit"; return EXFEM_E_STATE; }
-    if (rhs < 0 || rhs >= c.plan.R || npoint < 0 || (npoint > 0 && (!xy || !elem || !out))) {
+    if (rhs < 0 || rhs >= c.plan.R_user || npoint < 0 || (npoint > 0 && (!xy || !elem || !out))) {
         c.err = "bad sample_points arguments";
         return EXFEM_E_ARG;
     }
@@ -814,7 +819,9 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
     // (the sum over the allocations of setup_device, alloc_fp64/f32_alloc).
     if (!mesh || !prob) return 0;
     const size_t nn = (size_t)std::max(mesh->nnodes, 0), ne = (size_t)std::max(mesh->nelems, 0);
-    const size_t R = (size_t)std::max(prob->nrhs, 1), nh = (size_t)std::max(prob->nhanging, 0);
+    const bool pad = opts && opts->precision == EXFEM_FP32_KAHAN && opts->pad_rhs == 0;
+    const size_t R = (size_t)std::max(pad ? padded_rhs(prob->nrhs) : prob->nrhs, 1);
+    const size_t nh = (size_t)std::max(prob->nhanging, 0);
     const size_t ns = (size_t)std::max(prob->nseismic, 0), nr = (size_t)std::max(prob->nrecv, 0);
     const size_t nsave = prob->io_interval > 0 ? (size_t)(prob->nsteps / prob->io_interval + 1) : 1;
     size_t nabs = 0;

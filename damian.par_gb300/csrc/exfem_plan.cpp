@@ -237,7 +237,8 @@ static void radix_order(const uint64_t *key, int *idx, long long n) {
     for (long long i = 0; i < n; ++i) idx[i] = a[i].id;
 }
 
-int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &P, std::string &err) {
+int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &P, std::string &err,
+               int r_internal) {
     const int nn = mesh.nnodes, ne = mesh.nelems;
     if (nn <= 0 || ne <= 0 || !mesh.eptr || !mesh.eind || !mesh.ediv || !mesh.nodes || !mesh.ematprop) {
         err = "mesh arrays missing or empty";
@@ -271,7 +272,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         err = "mesh too large for 32-bit gather entries";
         return EXFEM_E_ARG;
     }
-    P.nn = nn; P.ne = ne; P.R = prob.nrhs;
+    P.nn = nn; P.ne = ne; P.R_user = prob.nrhs; P.R = std::max(prob.nrhs, r_internal);
     P.dt = prob.deltat;
     // setupconstants (explicit.f90:72-77)
     P.a1 = 1.0 / (P.dt * P.dt);
@@ -697,10 +698,11 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         if (e < 1 || e > ne) { err = "receiver " + std::to_string(i + 1) + " element out of range"; return EXFEM_E_ARG; }
     }
     if (int rc = point_weights(P, P.nrecv, prob.recv_xy, prob.recv_elem, P.rnode, P.rw, P.rsoil, err)) return rc;
-    // ---- waves (none: zero amplitudes, and no receiver adds a free field)
+    // ---- waves (none, or padding past the caller's: zero amplitudes, so their
+    // free field, DRM forces and receiver samples are zero)
     P.waves.resize(P.R);
     for (int r = 0; r < P.R; ++r) {
-        if (!prob.waves) {
+        if (!prob.waves || r >= P.R_user) {
             P.waves[r] = WaveConst();
             P.waves[r].kind = EXFEM_WAVE_P;
             P.waves[r].alpha = P.waves[r].beta = 1.0;

@@ -72,7 +72,7 @@ class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("use_graph", C.c_int),
                 ("graph_steps", C.c_int), ("block_threads", C.c_int),
                 ("rhs_per_thread", C.c_int), ("reorder", C.c_int), ("check_every", C.c_int),
-                ("variant", C.c_int), ("index_bits", C.c_int)]
+                ("variant", C.c_int), ("index_bits", C.c_int), ("pad_rhs", C.c_int)]
 
 
 class ModelInfo(C.Structure):

@@ -138,6 +138,11 @@ typedef struct exfem_opts {
     int index_bits;    /* FP32 direct gather: 0 = 32-bit indices when every
                           thread id and array index fits, else 64; 64 = always
                           64-bit (same results)                               */
+    int pad_rhs;       /* FP32 form: 0 = pad the right-hand sides to an even
+                          count (a multiple of 4 from 14) with zero-amplitude
+                          waves when that aligns the state rows; 1 = never.
+                          Same results; every output covers only the caller's
+                          right-hand sides                                    */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;

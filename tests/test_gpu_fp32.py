@@ -11,7 +11,7 @@ import pytest
 
 from exfem import decks, workloads
 from exfem.abi import EXFEM_E_NAN, EXFEM_FP32_KAHAN, ExfemError
-from exfem.gpu import Solver
+from exfem.gpu import Solver, estimate_bytes
 from exfem.model import Model
 from oracle import oracle
 from util import peak_rel, per_receiver_rel
@@ -137,6 +137,30 @@ def test_tiled_and_direct_kernels_agree():
     assert np.array_equal(a, b)
     for r in range(m.problem.nrhs):
         assert np.array_equal(ua[r], ub[r]), r
+
+
+def test_padded_rhs_match_unpadded():
+    """The FP32 form pads odd right-hand-side counts with zero-amplitude waves
+    (9 -> 10, 13 -> 16): the caller's seismograms and state are bit for bit
+    those of the unpadded run, every output covers only the caller's
+    right-hand sides, and the footprint estimate still bounds the context."""
+    for waves in (EIGHT_WAVES + [("WAVEP", 10.0)], EIGHT_WAVES + EIGHT_WAVES[:5]):
+        m = workloads.build("canyon", scale=0.2, steps=60, save_every=2, waves=waves)
+        R = m.problem.nrhs
+        assert R in (9, 13) and m.problem.nhanging > 0
+        a, ua = run32(m, pad_rhs=1)
+        b, ub = run32(m)
+        assert a.shape[0] == b.shape[0] == R
+        assert np.array_equal(a, b)
+        for r in range(R):
+            assert np.array_equal(ua[r], ub[r]), r
+        with Solver(m, precision=EXFEM_FP32_KAHAN) as s:
+            s.init_explicit()
+            assert estimate_bytes(m, precision=EXFEM_FP32_KAHAN) >= s.device_bytes
+            with pytest.raises(ExfemError):
+                s.u(R)
+        o = oracle.run(m, rhs=R - 1, nthreads=NT)
+        assert per_receiver_rel(b[R - 1], o["seis"]).max() <= TOL
 
 
 def test_get_u_copies_one_rhs():
