@@ -137,6 +137,17 @@ inline int spread_blocks(long long items, int per_block) {
     return (int)(b < 1 ? 1 : b);
 }
 
+// Device memory of a context: a stream-ordered allocation on its stream from
+// the library's memory pool for the device, which keeps what destroyed
+// contexts freed for the next ones (no cudaMalloc, and no cudaFree, which
+// waits for the whole device, once the pool has grown; see
+// exfem_gpu_release_cached).  ctx_alloc records the block for free_all and
+// counts it in the context's bytes; scratch_alloc does neither (free it with
+// cudaFreeAsync on the context's stream).
+cudaError_t ctx_alloc(Ctx &c, void **p, size_t bytes);
+cudaError_t scratch_alloc(Ctx &c, void **p, size_t bytes);
+int release_cached(int device);
+
 // Records a profiling mark after a launch (no-op unless profiling).
 void mark(Ctx &c, const char *kernel);
 

@@ -1009,9 +1009,7 @@ template <typename T, typename A>
 int upload32(Ctx &c, const std::vector<T, A> &v, const T **dst) {
     if (v.empty()) { *dst = nullptr; return EXFEM_OK; }
     void *p = nullptr;
-    CK(cudaMalloc(&p, v.size() * sizeof(T)));
-    c.allocs.push_back(p);
-    c.bytes += v.size() * sizeof(T);
+    CK(ctx_alloc(c, &p, v.size() * sizeof(T)));
     CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
     c.h2d_bytes += v.size() * sizeof(T);
     *dst = static_cast<const T *>(p);
@@ -1022,9 +1020,7 @@ template <typename T>
 int alloc32(Ctx &c, size_t n, T **dst) {
     void *p = nullptr;
     if (n == 0) n = 1;
-    CK(cudaMalloc(&p, n * sizeof(T)));
-    c.allocs.push_back(p);
-    c.bytes += n * sizeof(T);
+    CK(ctx_alloc(c, &p, n * sizeof(T)));
     *dst = static_cast<T *>(p);
     return EXFEM_OK;
 }

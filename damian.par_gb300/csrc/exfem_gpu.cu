@@ -19,7 +19,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -292,9 +294,7 @@ template <typename T, typename A>
 int upload(Ctx &c, const std::vector<T, A> &v, const T **dst) {
     if (v.empty()) { *dst = nullptr; return EXFEM_OK; }
     void *p = nullptr;
-    CK(cudaMalloc(&p, v.size() * sizeof(T)));
-    c.allocs.push_back(p);
-    c.bytes += v.size() * sizeof(T);
+    CK(ctx_alloc(c, &p, v.size() * sizeof(T)));
     CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
     c.h2d_bytes += v.size() * sizeof(T);
     *dst = static_cast<const T *>(p);
@@ -305,9 +305,7 @@ template <typename T>
 int dalloc(Ctx &c, size_t n, T **dst) {
     void *p = nullptr;
     if (n == 0) n = 1;
-    CK(cudaMalloc(&p, n * sizeof(T)));
-    c.allocs.push_back(p);
-    c.bytes += n * sizeof(T);
+    CK(ctx_alloc(c, &p, n * sizeof(T)));
     *dst = static_cast<T *>(p);
     return EXFEM_OK;
 }
@@ -406,9 +404,13 @@ int alloc_fp64(Ctx &c) {
 
 void free_all(Ctx &c) {
     if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
-    for (void *p : c.allocs) cudaFree(p);
+    if (c.stream) {
+        for (void *p : c.allocs) cudaFreeAsync(p, c.stream);   // back to the pool, in stream order
+        cudaStreamSynchronize(c.stream);
+        cudaStreamDestroy(c.stream);
+        c.stream = nullptr;
+    }
     c.allocs.clear();
-    if (c.stream) { cudaStreamDestroy(c.stream); c.stream = nullptr; }
 }
 
 int launch_step(Ctx &c, int par) {
@@ -462,6 +464,64 @@ int create_device(Ctx &c, const exfem_mesh &mesh) {
 }  // namespace
 
 namespace exfem {
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[128] = {};
+
+// The library's pool for a device, created on first use.  Its release
+// threshold keeps every freed byte, so contexts created after others were
+// destroyed reuse their memory.
+static cudaError_t device_pool(int dev, cudaMemPool_t *out) {
+    if (dev < 0 || dev >= 128) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        cudaError_t e = cudaMemPoolCreate(&pool, &props);
+        if (e != cudaSuccess) return e;
+        uint64_t keep = UINT64_MAX;
+        e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) { cudaMemPoolDestroy(pool); return e; }
+        g_pool[dev] = pool;
+    }
+    *out = g_pool[dev];
+    return cudaSuccess;
+}
+
+int release_cached(int device) {
+    cudaMemPool_t pool = nullptr;
+    {
+        if (device < 0 || device >= 128) return EXFEM_E_ARG;
+        std::lock_guard<std::mutex> lock(g_pool_mu);
+        pool = g_pool[device];
+    }
+    if (!pool) return EXFEM_OK;
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) return EXFEM_E_CUDA;
+    const cudaError_t e = cudaMemPoolTrimTo(pool, 0);
+    cudaSetDevice(prev);
+    return e == cudaSuccess ? EXFEM_OK : EXFEM_E_CUDA;
+}
+
+cudaError_t scratch_alloc(Ctx &c, void **p, size_t bytes) {
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = device_pool(c.device, &pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, c.stream);
+}
+
+cudaError_t ctx_alloc(Ctx &c, void **p, size_t bytes) {
+    cudaError_t e = scratch_alloc(c, p, bytes);
+    if (e == cudaSuccess) {
+        c.allocs.push_back(*p);
+        c.bytes += bytes;
+    }
+    return e;
+}
+
 void mark(Ctx &c, const char *kernel) {
     if (!c.prof_on) return;
     cudaEvent_t ev = nullptr;
@@ -654,7 +714,7 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     const long long ndof = 2LL * P.nn;
     std::vector<double> in((size_t)ndof);
     double *d = nullptr;
-    CK(cudaMalloc(&d, (size_t)ndof * sizeof(double)));
+    CK(scratch_alloc(c, reinterpret_cast<void **>(&d), (size_t)ndof * sizeof(double)));
     const bool f64 = c.precision == EXFEM_FP64;
     k_extract_rhs<<<nblocks(ndof, 256), 256, 0, c.stream>>>(f64 ? c.u64[c.parity] : nullptr,
                                                             f64 ? nullptr : c.uhi[c.parity], c.ucomp, P.R, rhs,
@@ -662,8 +722,8 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     c.launches++;
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(in.data(), d, (size_t)ndof * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    cudaFreeAsync(d, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-    cudaFree(d);
     if (e != cudaSuccess) { c.err = std::string("get_u: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
     c.d2h_bytes += (size_t)ndof * sizeof(double);
     for (int i = 0; i < P.nn; ++i) {
@@ -774,7 +834,7 @@ int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *x
     const size_t n = (size_t)npoint;
     const size_t bytes = n * (16 + 4) + n * (32 + 16 + 16) + 64;
     void *buf = nullptr;
-    CK(cudaMalloc(&buf, bytes));
+    CK(scratch_alloc(c, &buf, bytes));
     char *b = static_cast<char *>(buf);
     double *d_w = reinterpret_cast<double *>(b);
     double *d_xy = d_w + 4 * n;
@@ -795,8 +855,8 @@ int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *x
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, 16 * n, cudaMemcpyDeviceToHost, c.stream);
+    cudaFreeAsync(buf, c.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-    cudaFree(buf);
     c.h2d_bytes += n * (32 + 16 + 16 + 4);
     c.d2h_bytes += n * 16;
     if (e != cudaSuccess) { c.err = std::string("sample_points: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
@@ -806,6 +866,8 @@ int exfem_gpu_sample_points(exfem_ctx *ctx, int rhs, int npoint, const double *x
 int exfem_gpu_steps_done(const exfem_ctx *ctx) { return ctx ? ctx->steps_done : 0; }
 long long exfem_gpu_launch_count(const exfem_ctx *ctx) { return ctx ? ctx->launches : 0; }
 size_t exfem_gpu_device_bytes(const exfem_ctx *ctx) { return ctx ? ctx->bytes : 0; }
+
+int exfem_gpu_release_cached(int device) { return exfem::release_cached(device); }
 
 int exfem_gpu_copy_bytes(const exfem_ctx *ctx, unsigned long long *h2d, unsigned long long *d2h) {
     if (!ctx) return EXFEM_E_ARG;

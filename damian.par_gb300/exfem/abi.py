@@ -134,6 +134,7 @@ GPU_SYMBOLS = {
     "exfem_gpu_launch_count": (C.c_longlong, [C.c_void_p]),
     "exfem_gpu_device_bytes": (C.c_size_t, [C.c_void_p]),
     "exfem_gpu_copy_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]),
+    "exfem_gpu_release_cached": (C.c_int, [C.c_int]),
     "exfem_gpu_estimate_bytes": (C.c_size_t, [C.POINTER(Mesh), C.POINTER(Problem), C.POINTER(Opts)]),
     "exfem_gpu_last_error": (C.c_char_p, [C.c_void_p]),
     "exfem_gpu_destroy": (None, [C.c_void_p]),

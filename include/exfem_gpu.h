@@ -246,6 +246,13 @@ long long exfem_gpu_launch_count(const exfem_ctx *ctx);
 /* Bytes of device memory held by the context. */
 size_t exfem_gpu_device_bytes(const exfem_ctx *ctx);
 
+/* Contexts take their device memory from a stream-ordered pool per device
+ * that keeps what destroyed contexts freed, so later contexts (a server's
+ * next requests) reuse it without cudaMalloc/cudaFree.  This returns the
+ * pool's unused memory on `device` to the driver (memory of live contexts
+ * stays). */
+int exfem_gpu_release_cached(int device);
+
 /* Bytes the context has copied host -> device (the model's arrays at create,
  * sample points) and device -> host (seismograms, fields, status flags) so
  * far.  Either pointer may be NULL. */

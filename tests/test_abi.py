@@ -52,6 +52,7 @@ def test_argument_errors_need_no_device():
     bad = default_opts(block_threads=512)   # FP64 kernels take at most 256
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
     assert default_opts().index_bits == 0
+    assert L.exfem_gpu_release_cached(-1) == EXFEM_E_ARG
     bad = default_opts(index_bits=32)   # 0 (automatic) or 64
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
     assert b"index_bits" in L.exfem_gpu_last_error(None)

@@ -102,6 +102,29 @@ def test_estimate_bounds_every_form_and_copies_are_counted():
                     assert held < held64
 
 
+def test_pool_reuse_and_release():
+    """Contexts draw their device memory from the library's pool, which keeps
+    what destroyed contexts freed: repeated contexts give the same results,
+    and after exfem_gpu_release_cached hands the unused memory back, a new
+    context allocates afresh and again gives the same results."""
+    from exfem.gpu import gpu_lib
+    m = workloads.build("canyon", scale=0.2, steps=40)
+    outs = []
+    for _ in range(3):
+        with Solver(m, precision=EXFEM_FP32_KAHAN) as s:
+            s.init_explicit()
+            s.run()
+            s.sync()
+            outs.append(s.seismograms())
+    assert gpu_lib().exfem_gpu_release_cached(0) == 0
+    with Solver(m, precision=EXFEM_FP32_KAHAN) as s:
+        s.init_explicit()
+        s.run()
+        s.sync()
+        outs.append(s.seismograms())
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+
+
 def test_failures_stay_isolated():
     good, n = mix()[0]
     bad = Model(decks.homogeneous_rectangle(scale=0.125, steps=50, angle=0.6), nsteps=50)   # SV past critical
