@@ -163,6 +163,26 @@ def test_padded_rhs_match_unpadded():
         assert per_receiver_rel(b[R - 1], o["seis"]).max() <= TOL
 
 
+@pytest.mark.parametrize("nrhs", [96, 128])
+def test_many_rhs_match_oracle_and_fewer_rhs(nrhs):
+    """Batches wider than the 64-RHS valley: at four RHS per thread a node
+    takes 24 threads (R = 96, not a power of two) or 32 (R = 128, a whole
+    warp).  The first and last RHS match the oracle, and every RHS is bit for
+    bit the same as in a 16-RHS batch of the same waves."""
+    waves = [("WAVEP" if i % 2 == 0 else "WAVESV", (3.0 + 0.4 * i) % 25.0) for i in range(nrhs)]
+    m = workloads.build("canyon", scale=0.15, steps=120, save_every=2, waves=waves)
+    assert m.problem.nrhs == nrhs
+    g, u = run32(m)
+    for r in (0, nrhs - 1):
+        o = oracle.run(m, rhs=r, nthreads=NT)
+        assert per_receiver_rel(g[r], o["seis"]).max() <= TOL, r
+    m16 = workloads.build("canyon", scale=0.15, steps=120, save_every=2, waves=waves[nrhs - 16:])
+    g16, u16 = run32(m16)
+    assert np.array_equal(g[nrhs - 16:], g16)
+    for k in range(16):
+        assert np.array_equal(u[nrhs - 16 + k], u16[k])
+
+
 def test_get_u_copies_one_rhs():
     """exfem_gpu_get_u gathers the requested right-hand side on the device:
     2 * nnodes doubles cross to the host, not the batched state (FP32 and
