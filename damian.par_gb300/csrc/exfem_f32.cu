@@ -895,10 +895,14 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
                                                 int nb_recv, int ipb_drm) {
     int step = (mode == 1) ? 0 : read_step(m) + 1;
     const size_t R = m.R;
-    if ((int)blockIdx.x >= nb_hang + nb_recv) {
-        drm32_items(m, ipb_drm, (long long)blockIdx.x - nb_hang - nb_recv, step + 1);
-    } else if ((int)blockIdx.x < nb_hang) {
-        long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // the DRM blocks, whose FP64/exp chains are the longest, take the lowest
+    // block indices so that they are scheduled first
+    const int nb_drm = (int)gridDim.x - nb_hang - nb_recv;
+    const int bx = (int)blockIdx.x - nb_drm;
+    if (bx < 0) {
+        drm32_items(m, ipb_drm, blockIdx.x, step + 1);
+    } else if (bx < nb_hang) {
+        long long t = (long long)bx * blockDim.x + threadIdx.x;
         if (mode == 0 && t < (long long)m.n_hang * m.R) {
             int i = (int)(t / m.R), r = (int)(t % m.R);
             int h = m.hang[3 * i], a = m.hang[3 * i + 1], b = m.hang[3 * i + 2];
@@ -946,7 +950,7 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
         // term q (the FP64 Ricker pulses are the cost), thread 0 interpolates
         // and adds the terms in planewave_u's order; `ipb` items per block
         const int li = threadIdx.x >> 2;
-        const long long wq = (long long)(blockIdx.x - nb_hang) * ipb + li;
+        const long long wq = (long long)(bx - nb_hang) * ipb + li;
         const int q = (int)(threadIdx.x & 3);
         const bool valid = li < ipb && wq < (long long)m.nrecv * m.R;
         const int slot = step / m.io;
