@@ -271,6 +271,51 @@ def saturated_serving_leg(args, local):
                     "fp64 = plain FP64 GPU form, per-request ms/step x steps" % len(reqs)}
 
 
+def config4_leg(args, local):
+    """The serving config as specified: Poisson arrivals at 20/s of
+    problem.in texts (canyons and valleys of 1e4-3e6 elements, 1-16 angles,
+    1000-20000 steps), meshed and served by the server.  At these sizes the
+    offered load is many times one GPU's capacity, so latency is queueing;
+    throughput is the work over the makespan.  The plain FP64 form is timed
+    (10 steps after 3) on every `stride`-th request and the serial FP64 time
+    of the whole stream is the sampled seconds per unit of work times the
+    stream's work."""
+    from exfem import decks
+    from exfem.gpu import Solver
+    from exfem.model import Model
+    from exfem.serve import run_stream
+    stream = decks.serving_stream(n=args.config4_requests, rate=20.0, seed=11, min_scale=0.2, max_scale=1.0,
+                                  max_angles=16, step_range=(1000, 20000), canyon_nperlen=25.0, valley_chper=0.045)
+    recs, summary, _ = run_stream(stream, server_kw={"max_active": 16, "chunk_steps": 256, "device": local},
+                                  timeout=3000.0)
+    ok = [r for r in recs.values() if r.get("status") == 0]
+    sizes = sorted(r["nelems"] for r in ok)
+    work = sum(r["nelems"] * r["nrhs"] * r["nsteps"] for r in ok)
+    stride = max(1, len(stream) // 32)
+    w64 = t64 = 0.0
+    for _, d, n in stream[::stride]:
+        m = Model(d, nsteps=n)
+        with Solver(m, device=local) as s:
+            s.init_explicit()
+            s.run(3)
+            s.sync()
+            ms = C.c_double(0)
+            if s.lib.exfem_gpu_run_timed(s.h, 10, C.byref(ms)) != 0:
+                break
+        w64 += m.nelems * m.problem.nrhs * n
+        t64 += n * ms.value / 10.0 / 1000.0
+    fp64 = w64 / t64 if t64 > 0 else None
+    summary.update({"mode": "serving_config4", "work": work, "elements_min": sizes[0] if sizes else None,
+                    "elements_p50": sizes[len(sizes) // 2] if sizes else None,
+                    "elements_max": sizes[-1] if sizes else None,
+                    "offered_load": 20.0 * work / max(len(ok), 1),
+                    "fp64_throughput_sampled": fp64, "fp64_sample_requests": len(stream[::stride]),
+                    "ratio_served_fp32_over_fp64": summary["throughput"] / fp64 if fp64 else None,
+                    "note": "%d requests, Poisson 20/s, 1-16 angles, 1000-20000 steps, meshed by the server; "
+                            "plain FP64 timed on every %d-th request" % (len(stream), stride)})
+    return summary
+
+
 def run_reference(args, ws, rank, dist):
     if rank != 0:
         return
@@ -448,11 +493,17 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--serve-burst", type=int, default=16, help="requests in the saturated serving sample (0: skip)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
+    ap.add_argument("--serve-config4", action="store_true",
+                    help="only the serving config as specified (512 requests, minutes of GPU time); prints its own line")
+    ap.add_argument("--config4-requests", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local, dist, torch = dist_setup()
-    if args.impl == "reference":
+    if args.serve_config4:
+        if rank == 0:
+            print(json.dumps(config4_leg(args, local)))
+    elif args.impl == "reference":
         run_reference(args, ws, rank, dist)
     else:
         run_ours(args, ws, rank, local, dist, torch)
