@@ -209,7 +209,12 @@ __device__ __forceinline__ void drm32_items(const DevModel &m, int ipb, long lon
 // (checked on the host), so the index arithmetic is 32-bit and a power-of-two
 // thread count per node splits by shift and mask; this kernel is sensitive to
 // its instruction count (64-bit indices cost 7% on the 64-RHS valley).
-template <int RPT, bool I32>
+// TC: corners from the per-term copy m.tcorn (16 B per term) or, without it,
+// from the element's econn entry after the term (a longer chain, but econn is
+// shared by the element's four nodes through the caches).  At one or two RHS
+// the copy is most of the node's traffic: econn measured 12% faster on the
+// 1.5M-element valley with one RHS, the copy 1-2% faster from six.
+template <int RPT, bool I32, bool TC = true>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
                                                 unsigned short *__restrict__ dc) {
@@ -282,10 +287,12 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     const float4 *coef4 = reinterpret_cast<const float4 *>(m.ecoef32);
     for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
         int ent = __ldg(m.tlist + q);
-        int4 cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn) + q);
+        int4 cn;
+        if constexpr (TC) cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn) + q);
         float w = (ent & 1) ? 0.5f : 1.0f;
         int ec = ent >> 1;
         int e = ec >> 2, c = ec & 3;
+        if constexpr (!TC) cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + e);
         float4 k = __ldg(coef4 + e);
         const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
         float ux[4][RPT], uy[4][RPT];
@@ -1215,9 +1222,10 @@ int f32_alloc(Ctx &c) {
     if (c.opts.variant == 2 && P.R % 4 == 0) {
         if ((rc = pipe_setup(c))) return rc;
     }
-    // the direct gather's per-term corner copies
+    // the direct gather's per-term corner copies (from three RHS: with one or
+    // two, k_step32 reads the corners from econn)
     m.tcorn = nullptr;
-    if (!c.use_tiles && !c.use_pipe) {
+    if (!c.use_tiles && !c.use_pipe && P.R > 2) {
         pvec<int> tc;
         tc.resize(4 * std::max<size_t>(P.tlist.size(), 1));
         if (P.tlist.empty()) std::fill(tc.begin(), tc.end(), 0);
@@ -1285,7 +1293,15 @@ int f32_launch_step(Ctx &c, int par) {
         mark(c, "k_tile32");
     } else {
     const int nb = nblocks(work, T);
-    if (c.idx32) {
+    if (!m.tcorn) {   // one or two RHS: corners from econn
+        if (rpt == 2) {
+            if (c.idx32) k_step32<2, true, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+            else k_step32<2, false, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+        } else {
+            if (c.idx32) k_step32<1, true, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+            else k_step32<1, false, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+        }
+    } else if (c.idx32) {
         switch (rpt) {
             case 4: k_step32<4, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
             case 2: k_step32<2, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
