@@ -56,3 +56,20 @@ def test_argument_errors_need_no_device():
     bad = default_opts(index_bits=32)   # 0 (automatic) or 64
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
     assert b"index_bits" in L.exfem_gpu_last_error(None)
+
+
+def test_estimate_counts_rhs_padding():
+    """exfem_gpu_estimate_bytes needs no device.  An FP32 context pads an odd
+    right-hand-side count (13 -> 16) unless pad_rhs = 1, and its footprint
+    estimate grows with the padding; FP64 contexts never pad."""
+    from exfem import workloads
+    from exfem.gpu import estimate_bytes
+    waves = [("WAVEP" if i % 2 == 0 else "WAVESV", 2.0 * i) for i in range(13)]
+    m = workloads.build("canyon", scale=0.1, steps=10, waves=waves)
+    assert m.problem.nrhs == 13
+    padded = estimate_bytes(m, precision=1)
+    plain = estimate_bytes(m, precision=1, pad_rhs=1)
+    assert padded > plain
+    assert estimate_bytes(m, precision=0) == estimate_bytes(m, precision=0, pad_rhs=1)
+    even = workloads.build("canyon", scale=0.1, steps=10, waves=waves[:12])
+    assert estimate_bytes(even, precision=1) == estimate_bytes(even, precision=1, pad_rhs=1)
