@@ -55,6 +55,7 @@ struct DevModel {
     const float *hcoef4;           // per hanging entry: -2 a2 C (x, y), a1 M + a2 C (x, y)
     float *fdrm32;                 // ns * 8 * R DRM forces (FP64 math, stored FP32)
     const int *tcorn;              // 4 per gather term: the corners of its element
+    const double *drm_delay;       // ((s*4 + corner)*3 + term)*R + r: the DRM corners' free-field delays
     // point source (EXFEM_POINT_*; 0 = none)
     int point_kind, npoint;
     double point_amp, point_sigma, point_t0;

@@ -263,13 +263,19 @@ __host__ __device__ __forceinline__ void drm_forces(const T k[4], T mass, unsign
 // time t - (x sin + z cos)/v is formed in FP64 (the subtraction cancels), the
 // Ricker terms in FP32.  Relative error ~1e-7, the size of storing the forces
 // in FP32.
-__host__ __device__ __forceinline__ void planewave32(const DevWave &w, double t, double x1, double x3, float u[2],
-                                                     float a[2]) {
-    double v[3];
+// The FP32 free field's three travel-time delays at (x1, x3): incident,
+// reflected P, reflected SV.  They do not depend on time, so the FP32 DRM pass
+// reads them precomputed per (DRM corner, rhs) instead of redoing this FP64
+// arithmetic every step.
+__host__ __device__ __forceinline__ void planewave32_delays(const DevWave &w, double x1, double x3, double v[3]) {
     if (w.kind == EXFEM_WAVE_P) v[0] = (x1 * w.sine - x3 * w.cose) * w.inv_alpha;
     else v[0] = (x1 * w.sinf - x3 * w.cosf) * w.inv_beta;
     v[1] = (x1 * w.sine + x3 * w.cose) * w.inv_alpha;
     v[2] = (x1 * w.sinf + x3 * w.cosf) * w.inv_beta;
+}
+// planewave32 from its delays.
+__host__ __device__ __forceinline__ void planewave32_at(const DevWave &w, double t, const double v[3], float u[2],
+                                                        float a[2]) {
     const float fp2 = (float)(w.fp * w.fp);
     const float amp[3] = {(float)w.amp0, (float)w.wa1, (float)w.wb1};
     u[0] = u[1] = a[0] = a[1] = 0.f;
@@ -286,6 +292,12 @@ __host__ __device__ __forceinline__ void planewave32(const DevWave &w, double t,
         a[0] += r2 * ax;
         a[1] += r2 * az;
     }
+}
+__host__ __device__ __forceinline__ void planewave32(const DevWave &w, double t, double x1, double x3, float u[2],
+                                                     float a[2]) {
+    double v[3];
+    planewave32_delays(w, x1, x3, v);
+    planewave32_at(w, t, v, u, a);
 }
 
 }  // namespace exfem

@@ -182,8 +182,9 @@ __device__ __forceinline__ void drm32_items(const DevModel &m, int ipb, long lon
         const DevWave &wv = m.waves[r];
         double outt = (double)step * m.dt - wv.t0;
         ie = m.s_elem[s];
-        int x = m.econn[4 * ie + k];
-        planewave32(wv, outt, m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, uk, ak);
+        const double *dl = m.drm_delay + ((size_t)s * 4 + k) * 3 * m.R + r;
+        const double v[3] = {dl[0], dl[m.R], dl[2 * (size_t)m.R]};
+        planewave32_at(wv, outt, v, uk, ak);
     }
     float u0[8], a0[8];
 #pragma unroll
@@ -200,6 +201,20 @@ __device__ __forceinline__ void drm32_items(const DevModel &m, int ipb, long lon
     drm_forces<float>(kc, (float)m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
     m.fdrm32[((size_t)s * 8 + 2 * k) * m.R + r] = p[2 * k];
     m.fdrm32[((size_t)s * 8 + 2 * k + 1) * m.R + r] = p[2 * k + 1];
+}
+
+// Free-field delays of the DRM corners, once per context (see
+// planewave32_delays): thread per (DRM element, corner, rhs).
+__global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)m.ns * 4 * m.R) return;
+    const int r = (int)(t % m.R);
+    const long long sk = t / m.R;
+    const int k = (int)(sk & 3), s = (int)(sk >> 2);
+    const int x = m.econn[4 * m.s_elem[s] + k];
+    double v[3];
+    planewave32_delays(m.waves[r], m.nxy[2 * x] - m.worigin_x, m.nxy[2 * x + 1] - m.worigin_y, v);
+    for (int q = 0; q < 3; ++q) out[((size_t)s * 4 + k) * 3 * m.R + (size_t)q * m.R + r] = v[q];
 }
 
 // The fused step for one non-hanging node and RPT right-hand sides.  The
@@ -1145,6 +1160,15 @@ int f32_alloc(Ctx &c) {
     if ((rc = upload32(c, hc, &m.hcoef4))) return rc;
     if ((rc = upload32(c, P.ecoef32, &m.ecoef32))) return rc;
     if ((rc = alloc32(c, (size_t)std::max(m.ns, 1) * 8 * P.R, &m.fdrm32))) return rc;
+    m.drm_delay = nullptr;
+    if (m.ns > 0) {
+        double *dd = nullptr;
+        if ((rc = alloc32(c, (size_t)m.ns * 12 * P.R, &dd))) return rc;
+        k_drm_delays32<<<nblocks((long long)m.ns * 4 * P.R, 128), 128, 0, c.stream>>>(m, dd);
+        c.launches++;
+        CK(cudaGetLastError());
+        m.drm_delay = dd;
+    }
     size_t nst = (size_t)P.nn * 2 * P.R;
     if ((rc = alloc32(c, nst, &c.uhi[0]))) return rc;
     if ((rc = alloc32(c, nst, &c.uhi[1]))) return rc;

@@ -903,7 +903,7 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
     b += 16 * std::max(ns, (size_t)1) * R * 8;                      // DRM forces
     b += R * nsave * std::max(nr, (size_t)1) * 16 + 16;            // seismograms, counters
     if (f64) b += R * (nn * 32 + ne * 64);                          // u ping-pong, element forces
-    else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 32 * std::max(ns, (size_t)1) * R +
+    else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 32 * std::max(ns, (size_t)1) * R + 96 * ns * R +
               R * nn * 2 * (4 + 4 + 2 + 4 + 2);                     // FP32 state
     if (!f64 && opts->variant >= 1) {
         // tiles: every halo entry is a node or a corner/anchor of one of its terms
