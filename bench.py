@@ -271,6 +271,29 @@ def saturated_serving_leg(args, local):
                     "fp64 = plain FP64 GPU form, per-request ms/step x steps" % len(reqs)}
 
 
+def accuracy_leg(args, local):
+    """Seismogram error of the FP32 form against the plain FP64 form at full
+    length: the valley mesh with one SV wave (1.5M elements at scale 1, 20000
+    steps), relative L2 and peak amplitude per receiver (the same metrics as
+    the tests, tests/util.py)."""
+    from exfem import workloads
+    from exfem.gpu import Solver
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    from util import peak_rel, per_receiver_rel
+    m = workloads.build("valley", scale=args.scale, steps=args.accuracy_steps)
+    seis = {}
+    for prec in (1, 0):
+        with Solver(m, precision=prec, device=local) as s:
+            s.init_explicit()
+            s.run()
+            s.sync()
+            seis[prec] = s.seismograms()
+    return {"workload": "valley", "elements": m.nelems, "rhs": m.problem.nrhs, "steps": m.problem.nsteps,
+            "max_rel_l2": float(per_receiver_rel(seis[1][0], seis[0][0]).max()),
+            "max_peak_rel": float(peak_rel(seis[1][0], seis[0][0]).max()),
+            "against": "plain FP64 GPU form (matches the oracle to 1e-12)", "tolerance": 1e-4}
+
+
 def config4_leg(args, local):
     """The serving config as specified: Poisson arrivals at 20/s of
     problem.in texts (canyons and valleys of 1e4-3e6 elements, 1-16 angles,
@@ -455,6 +478,7 @@ def run_ours(args, ws, rank, local, dist, torch):
         del mf
 
     serving = serving_leg(args, local) if args.serve_requests > 0 else None
+    accuracy = accuracy_leg(args, local) if (not fp64 and args.accuracy_steps > 0 and rank == 0) else None
     if serving is not None and args.serve_burst > 0:
         serving["saturated"] = saturated_serving_leg(args, local)
 
@@ -471,6 +495,7 @@ def run_ours(args, ws, rank, local, dist, torch):
                             % ((2 * m.nnodes * R * (8 if fp64 else 4) * (2 if fp64 else 4)) / 1e6),
                       "parallelism": "replicas" if ws > 1 else "single"},
            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+           "accuracy": accuracy,
            "tuned": tuned or None, "plain_fp64": fp64_ref, "serving": serving}
     print(json.dumps(out))
 
@@ -493,6 +518,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--serve-burst", type=int, default=16, help="requests in the saturated serving sample (0: skip)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
+    ap.add_argument("--accuracy-steps", type=int, default=20000,
+                    help="steps of the FP32-vs-FP64 seismogram comparison on the valley (0: skip)")
     ap.add_argument("--serve-config4", action="store_true",
                     help="only the serving config as specified (512 requests, minutes of GPU time); prints its own line")
     ap.add_argument("--config4-requests", type=int, default=512)
