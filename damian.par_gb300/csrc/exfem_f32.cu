@@ -155,6 +155,76 @@ struct Half<4> {
     }
 };
 
+// A node's x and y rows (or a DRM corner's force pair) for RPT right-hand
+// sides starting at p (x) and p + R (y).  PAIR: the thread holds all of the
+// node's right-hand sides (RPT == R), so the two rows are adjacent and move
+// as one vector of 2 RPT values (8 or 16 bytes, aligned since p is a
+// multiple of 2 R).
+template <int RPT, bool PAIR>
+struct XY {
+    static_assert(!PAIR || RPT <= 2, "paired rows are one vector of at most 4 floats");
+    template <typename I>
+    __device__ static void load(const float *p, I R, float *x, float *y) {
+        if constexpr (PAIR) {
+            float t[2 * RPT];
+            Vec<2 * RPT>::load(p, t);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) { x[j] = t[j]; y[j] = t[RPT + j]; }
+        } else {
+            Vec<RPT>::load(p, x);
+            Vec<RPT>::load(p + R, y);
+        }
+    }
+    template <typename I>
+    __device__ static void load_cg(const float *p, I R, float *x, float *y) {
+        if constexpr (PAIR) {
+            float t[2 * RPT];
+            Vec<2 * RPT>::load_cg(p, t);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) { x[j] = t[j]; y[j] = t[RPT + j]; }
+        } else {
+            Vec<RPT>::load_cg(p, x);
+            Vec<RPT>::load_cg(p + R, y);
+        }
+    }
+    template <typename I>
+    __device__ static void store(float *p, I R, const float *x, const float *y) {
+        if constexpr (PAIR) {
+            float t[2 * RPT];
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) { t[j] = x[j]; t[RPT + j] = y[j]; }
+            Vec<2 * RPT>::store(p, t);
+        } else {
+            Vec<RPT>::store(p, x);
+            Vec<RPT>::store(p + R, y);
+        }
+    }
+    template <typename I>
+    __device__ static void load_half(const unsigned short *p, I R, float *x, float *y) {
+        if constexpr (PAIR) {
+            float t[2 * RPT];
+            Half<2 * RPT>::load(p, t);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) { x[j] = t[j]; y[j] = t[RPT + j]; }
+        } else {
+            Half<RPT>::load(p, x);
+            Half<RPT>::load(p + R, y);
+        }
+    }
+    template <typename I>
+    __device__ static void store_half(unsigned short *p, I R, const float *x, const float *y) {
+        if constexpr (PAIR) {
+            float t[2 * RPT];
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) { t[j] = x[j]; t[RPT + j] = y[j]; }
+            Half<2 * RPT>::store(p, t);
+        } else {
+            Half<RPT>::store(p, x);
+            Half<RPT>::store(p + R, y);
+        }
+    }
+};
+
 __device__ __forceinline__ float bf2f(unsigned short h) { return __bfloat162float(__ushort_as_bfloat16(h)); }
 __device__ __forceinline__ unsigned short f2bf(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
 
@@ -229,7 +299,9 @@ __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
 // shared by the element's four nodes through the caches).  At one or two RHS
 // the copy is most of the node's traffic: econn measured 12% faster on the
 // 1.5M-element valley with one RHS, the copy 1-2% faster from six.
-template <int RPT, bool I32, bool TC = true>
+// PAIR: one thread per node (RPT == R, one or two RHS), whose x and y rows
+// then load and store as one vector (XY).
+template <int RPT, bool I32, bool TC = true, bool PAIR = false>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
                                                 unsigned short *__restrict__ dc) {
@@ -262,6 +334,8 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     // takes the per-thread address work out of every warp (6% on the 64-RHS
     // valley); otherwise each thread prefetches its own lines, which measured
     // 8% faster at 4 and 1 right-hand sides per thread and slower at 2.
+    // Paired rows (one or two RHS, a node per thread) gain nothing from
+    // either form: measured the same with per-thread, bulk or no prefetches.
     if ((m.R & 3) == 0) {
         if (threadIdx.x == 0) {
             const long long tb = (long long)blockIdx.x * blockDim.x;
@@ -273,7 +347,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
             asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(dc + e0), "r"((unsigned)(cnt * 2)) : "memory");
             asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(uc + e0), "r"((unsigned)(cnt * 2)) : "memory");
         }
-    } else if (RPT != 2) {
+    } else if (RPT != 2 && !PAIR) {
         asm volatile("prefetch.global.L2 [%0];" ::"l"(dh + bn));
         asm volatile("prefetch.global.L2 [%0];" ::"l"(dh + bn + R));
         asm volatile("prefetch.global.L2 [%0];" ::"l"(dc + bn));
@@ -293,8 +367,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         int sc = ent >> 1;
         I b = ((I)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
         float fx[RPT], fy[RPT];
-        Vec<RPT>::load_cg(m.fdrm32 + b, fx);
-        Vec<RPT>::load_cg(m.fdrm32 + b + R, fy);
+        XY<RPT, PAIR>::load_cg(m.fdrm32 + b, R, fx, fy);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
     }
@@ -314,8 +387,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
             I b = ((I)cc[v] * 2) * R + r0;
-            Vec<RPT>::load(uh + b, ux[v]);
-            Vec<RPT>::load(uh + b + R, uy[v]);
+            XY<RPT, PAIR>::load(uh + b, R, ux[v], uy[v]);
         }
         const Q4Fold<float> f = q4_fold<float>(k.x, k.y, k.z, k.w, c, w);
 #pragma unroll
@@ -328,15 +400,13 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     // dashpot term -2 a2 C D (zero away from the absorbing boundary)
     const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
     float dx[RPT], dy[RPT];
-    Vec<RPT>::load_cg(dh + bn, dx);
-    Vec<RPT>::load_cg(dh + bn + R, dy);
+    XY<RPT, PAIR>::load_cg(dh + bn, R, dx, dy);
     if (nc.z != 0.f || nc.w != 0.f) {
 #pragma unroll
         for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
     }
     float unx[RPT], uny[RPT];
-    Vec<RPT>::load(uh + bn, unx);
-    Vec<RPT>::load(uh + bn + R, uny);
+    XY<RPT, PAIR>::load(uh + bn, R, unx, uny);
     // hanging nodes this node anchors:
     //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_h - u_n) + (D_h - D_n)) ]
     // (u_h, D_h from the hanging node's rows, which change only in k_hang32;
@@ -346,10 +416,8 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
         I bh = ((I)h * 2) * R + r0;
         float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
-        Vec<RPT>::load_cg(dh + bh, hx);
-        Vec<RPT>::load_cg(dh + bh + R, hy);
-        Vec<RPT>::load(uh + bh, uhx);
-        Vec<RPT>::load(uh + bh + R, uhy);
+        XY<RPT, PAIR>::load_cg(dh + bh, R, hx, hy);
+        XY<RPT, PAIR>::load(uh + bh, R, uhx, uhy);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
             ax[j] += 0.5f * (hc.x * hx[j] + hc.z * ((uhx[j] - unx[j]) + (hx[j] - dx[j])));
@@ -358,10 +426,8 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     }
     // delta = r / m_full; D+ = D + delta and u+ = u + D+, both Kahan-compensated
     float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
-    Half<RPT>::load(dc + bn, dcx);
-    Half<RPT>::load(dc + bn + R, dcy);
-    Half<RPT>::load(uc + bn, ucx);
-    Half<RPT>::load(uc + bn + R, ucy);
+    XY<RPT, PAIR>::load_half(dc + bn, R, dcx, dcy);
+    XY<RPT, PAIR>::load_half(uc + bn, R, ucx, ucy);
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         float yx = ax[j] * nc.x - dcx[j], yy = ay[j] * nc.y - dcy[j];
@@ -377,14 +443,10 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         ox[j] = sx;
         oy[j] = sy;
     }
-    Vec<RPT>::store(dh + bn, dx);
-    Vec<RPT>::store(dh + bn + R, dy);
-    Half<RPT>::store(dc + bn, dcx);
-    Half<RPT>::store(dc + bn + R, dcy);
-    Half<RPT>::store(uc + bn, ucx);
-    Half<RPT>::store(uc + bn + R, ucy);
-    Vec<RPT>::store(uhn + bn, ox);
-    Vec<RPT>::store(uhn + bn + R, oy);
+    XY<RPT, PAIR>::store(dh + bn, R, dx, dy);
+    XY<RPT, PAIR>::store_half(dc + bn, R, dcx, dcy);
+    XY<RPT, PAIR>::store_half(uc + bn, R, ucx, ucy);
+    XY<RPT, PAIR>::store(uhn + bn, R, ox, oy);
 }
 
 // Tiled variant of k_step32: a block owns `tn` consecutive active nodes (a
@@ -1061,9 +1123,11 @@ static int pick_rpt(const Ctx &c) {
     if (want == 1 || want == 2 || want == 4) return (R % want == 0) ? want : 1;
     // measured on canyons and valleys of 3e4-9e5 elements: two per thread
     // beats one from R = 4 (the per-term metadata and fold are shared), four
-    // pays off from R = 16
+    // pays off from R = 16.  At R = 2 two per thread make the node's x and y
+    // rows one 16-byte vector (k_step32's PAIR form): 17% faster per step on
+    // the 1.5M-element valley.
     if (R % 4 == 0 && R >= 16) return 4;
-    if (R % 2 == 0 && R >= 4) return 2;
+    if (R % 2 == 0) return 2;
     return 1;
 }
 
@@ -1317,10 +1381,13 @@ int f32_launch_step(Ctx &c, int par) {
         mark(c, "k_tile32");
     } else {
     const int nb = nblocks(work, T);
-    if (!m.tcorn) {   // one or two RHS: corners from econn
+    if (!m.tcorn) {   // one or two RHS: corners from econn, rows paired when RPT == R
         if (rpt == 2) {
-            if (c.idx32) k_step32<2, true, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-            else k_step32<2, false, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+            if (c.idx32) k_step32<2, true, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+            else k_step32<2, false, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+        } else if (m.R == 1) {
+            if (c.idx32) k_step32<1, true, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+            else k_step32<1, false, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
         } else {
             if (c.idx32) k_step32<1, true, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
             else k_step32<1, false, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);

@@ -225,6 +225,32 @@ def test_32_and_64_bit_indices_agree(rpt):
         assert np.array_equal(ua[r], ub[r]), r
 
 
+def test_paired_rows_match_split_rows():
+    """With one thread per node (one RHS, or two at two per thread) k_step32
+    moves a node's x and y rows as one vector; the terms and their order are
+    those of the split form.  Two RHS at one per thread (split rows) and at
+    two per thread (paired), and each RHS alone (paired), on a valley with
+    hanging nodes and a DRM layer: the same seismograms and state bit for
+    bit between the two-RHS runs, each RHS alone as in the batch (its wave's
+    delay is recomputed alone, hence 1e-6), and the oracle's seismograms
+    within the tolerance."""
+    waves = [("WAVESV", 0.0, 1.0, 5.0), ("WAVEP", math.radians(15.0), 1.0, 5.0)]
+    m = Model(decks.valley(scale=0.1, steps=2000, rhs=waves), nsteps=2000, io_interval=4)
+    assert m.problem.nhanging > 0 and m.problem.nseismic > 0 and m.problem.nrhs == 2
+    a, ua = run32(m, variant=0, rhs_per_thread=1)
+    b, ub = run32(m, variant=0, rhs_per_thread=2)
+    assert np.array_equal(a, b)
+    for r in range(2):
+        assert np.array_equal(ua[r], ub[r]), r
+    for r in range(2):
+        alone = Model(decks.valley(scale=0.1, steps=2000, rhs=[waves[r]]), nsteps=2000, io_interval=4)
+        c, _ = run32(alone, variant=0)
+        assert per_receiver_rel(c[0], a[r]).max() <= 1e-6, r
+        o = oracle.run(alone, nthreads=NT)
+        assert np.abs(o["seis"]).max() > 0.1
+        assert per_receiver_rel(c[0], o["seis"]).max() <= TOL, r
+
+
 EIGHT_WAVES = [("WAVEP", 0.0), ("WAVEP", 20.0), ("WAVEP", 40.0), ("WAVEP", 60.0),
                ("WAVESV", 0.0), ("WAVESV", 10.0), ("WAVESV", 20.0), ("WAVESV", 25.0)]
 
