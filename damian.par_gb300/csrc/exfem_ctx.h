@@ -138,6 +138,13 @@ inline int spread_blocks(long long items, int per_block) {
     return (int)(b < 1 ? 1 : b);
 }
 
+// FP32 direct gather: whether each term carries a copy of its element's
+// corners (16 B per term, one load less in the gather chain).  With few RHS
+// the copy is most of a node's traffic and the corners come from econn:
+// measured 12% faster with one RHS and, with a node's rows paired, 12% at
+// four (0.55M-element valley); the copy is 1-2% faster from six.
+inline bool f32_term_corners(int R) { return R > 4; }
+
 // Device memory of a context: a stream-ordered allocation on its stream from
 // the library's memory pool for the device, which keeps what destroyed
 // contexts freed for the next ones (no cudaMalloc, and no cudaFree, which

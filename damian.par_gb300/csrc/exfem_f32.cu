@@ -90,6 +90,27 @@ struct Vec<4> {
     }
 };
 
+// Eight floats (a paired node row at four RHS per thread) as one 32-byte
+// access; the address is 32-byte aligned.
+template <>
+struct Vec<8> {
+    __device__ static void load(const float *p, float *v) {
+        asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                     : "l"(p));
+    }
+    __device__ static void load_cg(const float *p, float *v) {
+        asm volatile("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                     : "l"(p) : "memory");
+    }
+    __device__ static void store(float *p, const float *v) {
+        asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+                     :: "l"(p), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+                     : "memory");
+    }
+};
+
 // RPT floats from shared memory.
 template <int N>
 struct VecS;
@@ -155,14 +176,34 @@ struct Half<4> {
     }
 };
 
+template <>
+struct Half<8> {
+    __device__ static void load(const unsigned short *p, float *v) {
+        uint4 w = *reinterpret_cast<const uint4 *>(p);
+        const unsigned u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[2 * k] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(u[k] & 0xffffu)));
+            v[2 * k + 1] = __bfloat162float(__ushort_as_bfloat16((unsigned short)(u[k] >> 16)));
+        }
+    }
+    __device__ static void store(unsigned short *p, const float *v) {
+        unsigned u[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            u[k] = (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * k])) |
+                   ((unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(v[2 * k + 1])) << 16);
+        *reinterpret_cast<uint4 *>(p) = make_uint4(u[0], u[1], u[2], u[3]);
+    }
+};
+
 // A node's x and y rows (or a DRM corner's force pair) for RPT right-hand
 // sides starting at p (x) and p + R (y).  PAIR: the thread holds all of the
 // node's right-hand sides (RPT == R), so the two rows are adjacent and move
-// as one vector of 2 RPT values (8 or 16 bytes, aligned since p is a
+// as one vector of 2 RPT values (8, 16 or 32 bytes, aligned since p is a
 // multiple of 2 R).
 template <int RPT, bool PAIR>
 struct XY {
-    static_assert(!PAIR || RPT <= 2, "paired rows are one vector of at most 4 floats");
     template <typename I>
     __device__ static void load(const float *p, I R, float *x, float *y) {
         if constexpr (PAIR) {
@@ -296,11 +337,10 @@ __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
 // its instruction count (64-bit indices cost 7% on the 64-RHS valley).
 // TC: corners from the per-term copy m.tcorn (16 B per term) or, without it,
 // from the element's econn entry after the term (a longer chain, but econn is
-// shared by the element's four nodes through the caches).  At one or two RHS
-// the copy is most of the node's traffic: econn measured 12% faster on the
-// 1.5M-element valley with one RHS, the copy 1-2% faster from six.
-// PAIR: one thread per node (RPT == R, one or two RHS), whose x and y rows
-// then load and store as one vector (XY).
+// shared by the element's four nodes through the caches); f32_term_corners
+// picks by RHS count.
+// PAIR: one thread per node (RPT == R: one, two or four RHS), whose x and y
+// rows then load and store as one vector (XY).
 template <int RPT, bool I32, bool TC = true, bool PAIR = false>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
@@ -1123,10 +1163,11 @@ static int pick_rpt(const Ctx &c) {
     if (want == 1 || want == 2 || want == 4) return (R % want == 0) ? want : 1;
     // measured on canyons and valleys of 3e4-9e5 elements: two per thread
     // beats one from R = 4 (the per-term metadata and fold are shared), four
-    // pays off from R = 16.  At R = 2 two per thread make the node's x and y
-    // rows one 16-byte vector (k_step32's PAIR form): 17% faster per step on
-    // the 1.5M-element valley.
-    if (R % 4 == 0 && R >= 16) return 4;
+    // pays off from R = 16.  At R = 2 and 4 a thread per node makes the
+    // node's x and y rows one 16- or 32-byte vector (k_step32's PAIR form):
+    // 17% faster per step than two threads per node on the 1.5M-element
+    // valley at R = 2, 12% on a 0.55M-element valley at R = 4.
+    if (R % 4 == 0 && (R >= 16 || R == 4)) return 4;
     if (R % 2 == 0) return 2;
     return 1;
 }
@@ -1313,7 +1354,7 @@ int f32_alloc(Ctx &c) {
     // the direct gather's per-term corner copies (from three RHS: with one or
     // two, k_step32 reads the corners from econn)
     m.tcorn = nullptr;
-    if (!c.use_tiles && !c.use_pipe && P.R > 2) {
+    if (!c.use_tiles && !c.use_pipe && f32_term_corners(P.R)) {
         pvec<int> tc;
         tc.resize(4 * std::max<size_t>(P.tlist.size(), 1));
         if (P.tlist.empty()) std::fill(tc.begin(), tc.end(), 0);
@@ -1345,6 +1386,13 @@ int f32_init(Ctx &c) {
         CK(cudaGetLastError());
     }
     return EXFEM_OK;
+}
+
+// k_step32 with 32- or 64-bit indices as the context allows.
+template <int RPT, bool TC, bool PAIR>
+static void step32(Ctx &c, int nb, int T, const float *uh, float *uhn) {
+    if (c.idx32) k_step32<RPT, true, TC, PAIR><<<nb, T, 0, c.stream>>>(c.dm, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+    else k_step32<RPT, false, TC, PAIR><<<nb, T, 0, c.stream>>>(c.dm, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
 }
 
 int f32_launch_step(Ctx &c, int par) {
@@ -1381,28 +1429,27 @@ int f32_launch_step(Ctx &c, int par) {
         mark(c, "k_tile32");
     } else {
     const int nb = nblocks(work, T);
-    if (!m.tcorn) {   // one or two RHS: corners from econn, rows paired when RPT == R
-        if (rpt == 2) {
-            if (c.idx32) k_step32<2, true, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-            else k_step32<2, false, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-        } else if (m.R == 1) {
-            if (c.idx32) k_step32<1, true, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-            else k_step32<1, false, false, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-        } else {
-            if (c.idx32) k_step32<1, true, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-            else k_step32<1, false, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-        }
-    } else if (c.idx32) {
+    if (!m.tcorn) {   // few RHS: corners from econn, rows paired when a thread holds the node
+        const bool pair = rpt == m.R;
         switch (rpt) {
-            case 4: k_step32<4, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-            case 2: k_step32<2, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-            default: k_step32<1, true><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            case 4:
+                if (pair) step32<4, false, true>(c, nb, T, uh, uhn);
+                else step32<4, false, false>(c, nb, T, uh, uhn);
+                break;
+            case 2:
+                if (pair) step32<2, false, true>(c, nb, T, uh, uhn);
+                else step32<2, false, false>(c, nb, T, uh, uhn);
+                break;
+            default:
+                if (pair) step32<1, false, true>(c, nb, T, uh, uhn);
+                else step32<1, false, false>(c, nb, T, uh, uhn);
+                break;
         }
     } else {
         switch (rpt) {
-            case 4: k_step32<4, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-            case 2: k_step32<2, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
-            default: k_step32<1, false><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;
+            case 4: step32<4, true, false>(c, nb, T, uh, uhn); break;
+            case 2: step32<2, true, false>(c, nb, T, uh, uhn); break;
+            default: step32<1, true, false>(c, nb, T, uh, uhn); break;
         }
     }
     c.launches++;

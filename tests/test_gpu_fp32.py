@@ -226,22 +226,35 @@ def test_32_and_64_bit_indices_agree(rpt):
 
 
 def test_paired_rows_match_split_rows():
-    """With one thread per node (one RHS, or two at two per thread) k_step32
-    moves a node's x and y rows as one vector; the terms and their order are
-    those of the split form.  Two RHS at one per thread (split rows) and at
-    two per thread (paired), and each RHS alone (paired), on a valley with
-    hanging nodes and a DRM layer: the same seismograms and state bit for
-    bit between the two-RHS runs, each RHS alone as in the batch (its wave's
-    delay is recomputed alone, hence 1e-6), and the oracle's seismograms
-    within the tolerance."""
-    waves = [("WAVESV", 0.0, 1.0, 5.0), ("WAVEP", math.radians(15.0), 1.0, 5.0)]
-    m = Model(decks.valley(scale=0.1, steps=2000, rhs=waves), nsteps=2000, io_interval=4)
+    """With one thread per node (one, two or four RHS at as many per thread)
+    k_step32 moves a node's x and y rows as one 8-, 16- or 32-byte vector;
+    the terms and their order are those of the split form.  On a valley with
+    hanging nodes and a DRM layer: two RHS at one per thread (split rows) and
+    at two (paired); four RHS at one and two per thread (split) and at four
+    (paired); three RHS (padded to four, paired) against the first three of
+    the four.  The same seismograms and state bit for bit; each of the two
+    RHS alone (paired) as in the batch (its wave's delay is recomputed alone,
+    hence 1e-6) and within the tolerance of the oracle."""
+    waves = [("WAVESV", 0.0, 1.0, 5.0), ("WAVEP", math.radians(15.0), 1.0, 5.0),
+             ("WAVESV", math.radians(10.0), 0.7, 3.0), ("WAVEP", math.radians(40.0), 1.2, 4.0)]
+    m = Model(decks.valley(scale=0.1, steps=2000, rhs=waves[:2]), nsteps=2000, io_interval=4)
     assert m.problem.nhanging > 0 and m.problem.nseismic > 0 and m.problem.nrhs == 2
     a, ua = run32(m, variant=0, rhs_per_thread=1)
     b, ub = run32(m, variant=0, rhs_per_thread=2)
     assert np.array_equal(a, b)
     for r in range(2):
         assert np.array_equal(ua[r], ub[r]), r
+    m4 = Model(decks.valley(scale=0.1, steps=600, rhs=waves), nsteps=600, io_interval=4)
+    runs = [run32(m4, variant=0, rhs_per_thread=rpt) for rpt in (1, 2, 4)]
+    for g, u in runs[1:]:
+        assert np.array_equal(g, runs[0][0])
+        for r in range(4):
+            assert np.array_equal(u[r], runs[0][1][r]), r
+    m3 = Model(decks.valley(scale=0.1, steps=600, rhs=waves[:3]), nsteps=600, io_interval=4)
+    g3, u3 = run32(m3, variant=0)
+    assert g3.shape[0] == 3 and np.array_equal(g3, runs[0][0][:3])
+    for r in range(3):
+        assert np.array_equal(u3[r], runs[0][1][r]), r
     for r in range(2):
         alone = Model(decks.valley(scale=0.1, steps=2000, rhs=[waves[r]]), nsteps=2000, io_interval=4)
         c, _ = run32(alone, variant=0)
