@@ -26,6 +26,7 @@ struct DevWave {
 // Device arrays common to both arithmetic forms.
 struct DevModel {
     int nn, ne, R, n_active, n_hang, ns, nrecv, nsave, io;
+    int lg;                  // RHS group of the state layout (row_off): R, or the FP32 RHS per thread
     double dt, a1, a2, a3;
     double worigin_x, worigin_y;
     const int *econn;        // 4 per element
@@ -144,6 +145,13 @@ inline int spread_blocks(long long items, int per_block) {
 // measured 12% faster with one RHS and, with a node's rows paired, 12% at
 // four (0.55M-element valley); the copy is 1-2% faster from six.
 inline bool f32_term_corners(int R) { return R > 4; }
+
+// FP32 direct gather with several threads per node: whether the state is laid
+// out in groups of one thread's right-hand sides (row_off), so that a thread's
+// x and y values of a node are adjacent and move as one vector.  Measured 9 to
+// 12% faster per step from 6 to 16 RHS on a 0.55M-element valley and on the
+// served requests; no gain at 64.
+inline bool f32_interleave(int R) { return R < 64; }
 
 // Device memory of a context: a stream-ordered allocation on its stream from
 // the library's memory pool for the device, which keeps what destroyed

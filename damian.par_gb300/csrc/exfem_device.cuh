@@ -7,6 +7,20 @@
 
 namespace exfem {
 
+// Offset of (dof d, rhs r) within a node's 2R state values, or within a DRM
+// corner's force pair.  The right-hand sides form groups of m.lg, and each
+// group holds its x row, then its y row.  lg = R is the plain layout (every
+// RHS's x, then every RHS's y); lg = the FP32 direct gather's RHS per thread
+// puts a thread's x and y values of a node side by side, so that it loads
+// and stores them as one vector.
+__host__ __device__ __forceinline__ size_t row_off(const DevModel &m, int d, int r) {
+    const int g = r / m.lg;
+    return (size_t)g * 2 * m.lg + (size_t)d * m.lg + (size_t)(r - g * m.lg);
+}
+__host__ __device__ __forceinline__ size_t state_at(const DevModel &m, size_t n, int d, int r) {
+    return n * 2 * (size_t)m.R + row_off(m, d, r);
+}
+
 // Q4 square plane-strain stiffness applied to one element's corner
 // displacements, K(mu, lambda) u with K = calck(mu, lambda)
 // (formulation.f90:276-313).  The bilinear field is split into its modes

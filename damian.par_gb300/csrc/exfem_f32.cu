@@ -26,9 +26,11 @@
 //   k_hang32   hanging nodes = anchor averages; receivers in FP64; and the
 //              next step's DRM effective forces (travel times FP64, stored
 //              FP32), which depend on time only
-// State layout: value (node n, dof d, rhs r) at (n*2 + d)*R + r, so a warp
-// reads R contiguous values per (node, dof) and one set of mesh metadata
-// serves every right-hand side.
+// State layout: a node's 2R values are contiguous, so one set of mesh
+// metadata serves every right-hand side.  Within them (row_off) the RHS form
+// groups of m.lg, each group's x row, then its y row: lg = R (plain:
+// (n*2 + d)*R + r), or lg = RHS per thread for the direct gather with
+// several threads per node, whose x and y values then sit side by side.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -197,11 +199,11 @@ struct Half<8> {
     }
 };
 
-// A node's x and y rows (or a DRM corner's force pair) for RPT right-hand
-// sides starting at p (x) and p + R (y).  PAIR: the thread holds all of the
-// node's right-hand sides (RPT == R), so the two rows are adjacent and move
-// as one vector of 2 RPT values (8, 16 or 32 bytes, aligned since p is a
-// multiple of 2 R).
+// A thread's x and y values of a node (or of a DRM corner's force pair) for
+// RPT right-hand sides: at p and p + R in the plain layout; PAIR: at p and
+// p + RPT in the layout grouped by RPT (row_off), where they move as one
+// vector of 2 RPT values (8, 16 or 32 bytes, aligned: p is a multiple of
+// 2 RPT).
 template <int RPT, bool PAIR>
 struct XY {
     template <typename I>
@@ -310,8 +312,8 @@ __device__ __forceinline__ void drm32_items(const DevModel &m, int ipb, long lon
     float kc[4] = {k4.x, k4.y, k4.z, k4.w};
     float p[8];
     drm_forces<float>(kc, (float)m.emass[ie], drm_mask(m.s_kind[s]), u0, a0, p);
-    m.fdrm32[((size_t)s * 8 + 2 * k) * m.R + r] = p[2 * k];
-    m.fdrm32[((size_t)s * 8 + 2 * k + 1) * m.R + r] = p[2 * k + 1];
+    m.fdrm32[((size_t)s * 8 + 2 * k) * m.R + row_off(m, 0, r)] = p[2 * k];
+    m.fdrm32[((size_t)s * 8 + 2 * k) * m.R + row_off(m, 1, r)] = p[2 * k + 1];
 }
 
 // Free-field delays of the DRM corners, once per context (see
@@ -339,8 +341,9 @@ __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
 // from the element's econn entry after the term (a longer chain, but econn is
 // shared by the element's four nodes through the caches); f32_term_corners
 // picks by RHS count.
-// PAIR: one thread per node (RPT == R: one, two or four RHS), whose x and y
-// rows then load and store as one vector (XY).
+// PAIR: the state is grouped by RPT (m.lg == RPT, row_off; with RPT == R
+// that is the plain layout), so the thread's x and y values of a node are
+// adjacent and load and store as one vector (XY).
 template <int RPT, bool I32, bool TC = true, bool PAIR = false>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
@@ -365,7 +368,10 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         r0 = (int)(t % G) * RPT;
     }
     const I R = m.R;
-    const I bn = ((I)n * 2) * R + r0;
+    // PAIR: the state is grouped by RPT (m.lg == RPT), so this thread's
+    // values of a node start at 2 r0 and its y row follows its x row
+    const I roff = PAIR ? 2 * (I)r0 : (I)r0;
+    const I bn = ((I)n * 2) * R + roff;
     // Ask L2 for the node's own streaming state (read only after the
     // gather) so its DRAM latency overlaps the gather instead of following
     // it.  A block's nodes are consecutive, so their rows are one range per
@@ -405,7 +411,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         int ent = __ldg(m.dlist + q);
         float w = (ent & 1) ? 0.5f : 1.0f;
         int sc = ent >> 1;
-        I b = ((I)(sc >> 2) * 8 + 2 * (sc & 3)) * R + r0;
+        I b = ((I)(sc >> 2) * 8 + 2 * (sc & 3)) * R + roff;
         float fx[RPT], fy[RPT];
         XY<RPT, PAIR>::load_cg(m.fdrm32 + b, R, fx, fy);
 #pragma unroll
@@ -426,7 +432,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         float ux[4][RPT], uy[4][RPT];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            I b = ((I)cc[v] * 2) * R + r0;
+            I b = ((I)cc[v] * 2) * R + roff;
             XY<RPT, PAIR>::load(uh + b, R, ux[v], uy[v]);
         }
         const Q4Fold<float> f = q4_fold<float>(k.x, k.y, k.z, k.w, c, w);
@@ -454,7 +460,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
         int h = __ldg(m.llist + 2 * q);
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
-        I bh = ((I)h * 2) * R + r0;
+        I bh = ((I)h * 2) * R + roff;
         float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
         XY<RPT, PAIR>::load_cg(dh + bh, R, hx, hy);
         XY<RPT, PAIR>::load(uh + bh, R, uhx, uhy);
@@ -952,7 +958,7 @@ __global__ void k_point32(DevModel m, const int *__restrict__ pn, const float *_
     if (t >= (long long)np * m.R) return;
     const int i = (int)(t / m.R), r = (int)(t % m.R);
     const int n = pn[i];
-    const size_t iy = ((size_t)n * 2 + 1) * m.R + r;
+    const size_t iy = state_at(m, (size_t)n, 1, r);
     const double f = point_value(m, read_step(m) + 1);
     const double u1 = (double)uhn[iy] - (double)bf2f(uc[iy]);
     const double d1 = (double)dh[iy] - (double)bf2f(dc[iy]);
@@ -979,7 +985,7 @@ __global__ void k_point_init32(DevModel m, float *__restrict__ uh, unsigned shor
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)m.npoint * m.R) return;
     const int n = m.pnodes[t / m.R], r = (int)(t % m.R);
-    const size_t iy = ((size_t)n * 2 + 1) * m.R + r;
+    const size_t iy = state_at(m, (size_t)n, 1, r);
     const double d = v0 - vm;
     const float uh2 = (float)v0, dh2 = (float)d;
     uh[iy] = uh2;
@@ -992,9 +998,8 @@ __global__ void k_point_init32(DevModel m, float *__restrict__ uh, unsigned shor
 // (rows: read a hanging corner's own row, for the step-0 sample.)
 __device__ __forceinline__ void load_u32(const DevModel &m, const float *uh, const unsigned short *uc, int node,
                                          int r, bool rows, double &vx, double &vy) {
-    const size_t R = m.R;
     auto val = [&](int x, int d) {
-        size_t i = ((size_t)x * 2 + d) * R + r;
+        size_t i = state_at(m, (size_t)x, d, r);
         return (double)uh[i] - (double)bf2f(uc[i]);
     };
     if (node < m.n_active || rows) {
@@ -1018,7 +1023,6 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
                                                 unsigned short *__restrict__ dc, int nb_hang, int mode, int ipb,
                                                 int nb_recv, int ipb_drm) {
     int step = (mode == 1) ? 0 : read_step(m) + 1;
-    const size_t R = m.R;
     // the DRM blocks, whose FP64/exp chains are the longest, take the lowest
     // block indices so that they are scheduled first
     const int nb_drm = (int)gridDim.x - nb_hang - nb_recv;
@@ -1043,9 +1047,9 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
             double u_old[2];
 #pragma unroll
             for (int d = 0; d < 2; ++d) {
-                ih[d] = ((size_t)h * 2 + d) * R + r;
-                ia[d] = ((size_t)a * 2 + d) * R + r;
-                ib[d] = ((size_t)b * 2 + d) * R + r;
+                ih[d] = state_at(m, (size_t)h, d, r);
+                ia[d] = state_at(m, (size_t)a, d, r);
+                ib[d] = state_at(m, (size_t)b, d, r);
                 u_old[d] = (double)uho[ih[d]] - (double)bf2f(uc[ih[d]]);   // the row before this step
                 ua[d] = uhn[ia[d]]; ub[d] = uhn[ib[d]];
                 uca[d] = uc[ia[d]]; ucb[d] = uc[ib[d]];
@@ -1351,10 +1355,14 @@ int f32_alloc(Ctx &c) {
     if (c.opts.variant == 2 && P.R % 4 == 0) {
         if ((rc = pipe_setup(c))) return rc;
     }
-    // the direct gather's per-term corner copies (from three RHS: with one or
-    // two, k_step32 reads the corners from econn)
+    // the direct gather with several threads per node groups the state by
+    // the thread's RHS (the tiled variants read the plain layout)
+    const bool direct = !c.use_tiles && !c.use_pipe;
+    m.lg = (direct && c.rhs_per_thread < P.R && f32_interleave(P.R)) ? c.rhs_per_thread : P.R;
+    // the direct gather's per-term corner copies (with few RHS k_step32
+    // reads the corners from econn)
     m.tcorn = nullptr;
-    if (!c.use_tiles && !c.use_pipe && f32_term_corners(P.R)) {
+    if (direct && f32_term_corners(P.R)) {
         pvec<int> tc;
         tc.resize(4 * std::max<size_t>(P.tlist.size(), 1));
         if (P.tlist.empty()) std::fill(tc.begin(), tc.end(), 0);
@@ -1429,8 +1437,10 @@ int f32_launch_step(Ctx &c, int par) {
         mark(c, "k_tile32");
     } else {
     const int nb = nblocks(work, T);
-    if (!m.tcorn) {   // few RHS: corners from econn, rows paired when a thread holds the node
-        const bool pair = rpt == m.R;
+    // rows paired when the state is grouped by the thread's RHS (or a thread
+    // holds the whole node)
+    const bool pair = m.lg == rpt;
+    if (!m.tcorn) {   // few RHS: corners from econn
         switch (rpt) {
             case 4:
                 if (pair) step32<4, false, true>(c, nb, T, uh, uhn);
@@ -1447,9 +1457,18 @@ int f32_launch_step(Ctx &c, int par) {
         }
     } else {
         switch (rpt) {
-            case 4: step32<4, true, false>(c, nb, T, uh, uhn); break;
-            case 2: step32<2, true, false>(c, nb, T, uh, uhn); break;
-            default: step32<1, true, false>(c, nb, T, uh, uhn); break;
+            case 4:
+                if (pair) step32<4, true, true>(c, nb, T, uh, uhn);
+                else step32<4, true, false>(c, nb, T, uh, uhn);
+                break;
+            case 2:
+                if (pair) step32<2, true, true>(c, nb, T, uh, uhn);
+                else step32<2, true, false>(c, nb, T, uh, uhn);
+                break;
+            default:
+                if (pair) step32<1, true, true>(c, nb, T, uh, uhn);
+                else step32<1, true, false>(c, nb, T, uh, uhn);
+                break;
         }
     }
     c.launches++;

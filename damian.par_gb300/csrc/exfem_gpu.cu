@@ -220,18 +220,18 @@ __global__ void k_sample_points(DevModel m, const double *__restrict__ u64, cons
                                 const double *__restrict__ xy, double time, double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    const size_t R = m.R;
     double fx = 0.0, fy = 0.0;
     if (node[4 * (size_t)i] >= 0) {
         for (int k = 0; k < 4; ++k) {
-            const size_t b = ((size_t)node[4 * (size_t)i + k] * 2) * R + rhs;
+            const size_t bx = state_at(m, (size_t)node[4 * (size_t)i + k], 0, rhs);
+            const size_t by = state_at(m, (size_t)node[4 * (size_t)i + k], 1, rhs);
             double vx, vy;
             if (u64) {
-                vx = u64[b];
-                vy = u64[b + R];
+                vx = u64[bx];
+                vy = u64[by];
             } else {
-                vx = (double)uh[b] - (double)__bfloat162float(__ushort_as_bfloat16(uc[b]));
-                vy = (double)uh[b + R] - (double)__bfloat162float(__ushort_as_bfloat16(uc[b + R]));
+                vx = (double)uh[bx] - (double)__bfloat162float(__ushort_as_bfloat16(uc[bx]));
+                vy = (double)uh[by] - (double)__bfloat162float(__ushort_as_bfloat16(uc[by]));
             }
             const double wk = w[4 * (size_t)i + k];
             fx = fx + wk * vx;
@@ -251,12 +251,12 @@ __global__ void k_sample_points(DevModel m, const double *__restrict__ u64, cons
 
 // One right-hand side of the state in internal dof order (2 per node): the
 // FP64 value, or u_hi - u_comp in FP64 for the FP32 form.
-__global__ void k_extract_rhs(const double *__restrict__ u64, const float *__restrict__ uh,
-                              const unsigned short *__restrict__ uc, int R, int rhs, long long ndof,
+__global__ void k_extract_rhs(DevModel m, const double *__restrict__ u64, const float *__restrict__ uh,
+                              const unsigned short *__restrict__ uc, int rhs, long long ndof,
                               double *__restrict__ out) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ndof) return;
-    const size_t k = (size_t)i * R + rhs;
+    const size_t k = state_at(m, (size_t)(i >> 1), (int)(i & 1), rhs);
     out[i] = u64 ? u64[k] : (double)uh[k] - (double)__bfloat162float(__ushort_as_bfloat16(uc[k]));
 }
 
@@ -320,6 +320,7 @@ int setup_device(Ctx &c) {
     Plan &P = c.plan;
     DevModel &m = c.dm;
     m.nn = P.nn; m.ne = P.ne; m.R = P.R; m.n_active = P.n_active; m.n_hang = P.n_hang;
+    m.lg = P.R;   // plain layout; the FP32 direct gather may group it (f32_alloc)
     m.ns = (int)P.s_elem.size(); m.nrecv = P.nrecv; m.nsave = P.nsave; m.io = P.io;
     m.dt = P.dt; m.a1 = P.a1; m.a2 = P.a2; m.a3 = P.a3;
     m.worigin_x = P.worigin[0]; m.worigin_y = P.worigin[1];
@@ -716,8 +717,8 @@ int exfem_gpu_get_u(exfem_ctx *ctx, int rhs, double *u, size_t n) {
     double *d = nullptr;
     CK(scratch_alloc(c, reinterpret_cast<void **>(&d), (size_t)ndof * sizeof(double)));
     const bool f64 = c.precision == EXFEM_FP64;
-    k_extract_rhs<<<nblocks(ndof, 256), 256, 0, c.stream>>>(f64 ? c.u64[c.parity] : nullptr,
-                                                            f64 ? nullptr : c.uhi[c.parity], c.ucomp, P.R, rhs,
+    k_extract_rhs<<<nblocks(ndof, 256), 256, 0, c.stream>>>(c.dm, f64 ? c.u64[c.parity] : nullptr,
+                                                            f64 ? nullptr : c.uhi[c.parity], c.ucomp, rhs,
                                                             ndof, d);
     c.launches++;
     cudaError_t e = cudaGetLastError();

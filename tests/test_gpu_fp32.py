@@ -264,6 +264,40 @@ def test_paired_rows_match_split_rows():
         assert per_receiver_rel(c[0], o["seis"]).max() <= TOL, r
 
 
+def test_grouped_layouts_agree():
+    """With several threads per node the direct gather groups each node's
+    state by the thread's RHS (x then y values of one, two or four RHS side
+    by side); the tiled kernel reads the plain layout.  Twelve RHS on a
+    valley with hanging nodes, a DRM layer and receivers, at one, two and
+    four RHS per thread and tiled: the same seismograms, state (get_u) and
+    sampled field (sample_points) of every RHS bit for bit, and the
+    oracle's seismograms within the tolerance."""
+    waves = [("WAVEP" if i % 2 == 0 else "WAVESV", math.radians(2.0 * i), 1.0, 5.0) for i in range(12)]
+    m = Model(decks.valley(scale=0.1, steps=1500, rhs=waves), nsteps=1500, io_interval=5)
+    assert m.problem.nhanging > 0 and m.problem.nseismic > 0 and m.problem.nrhs == 12
+    xy = m.nodes().reshape(-1, 2)
+    grid = m.grid(0.0, xy[:, 0].max(), 0.0, xy[:, 1].max(), 40.0)
+    assert grid["nfound"] > 0
+    runs = []
+    for opts in (dict(rhs_per_thread=1), dict(rhs_per_thread=2), dict(rhs_per_thread=4), dict(variant=1)):
+        with Solver(m, precision=EXFEM_FP32_KAHAN, **opts) as s:
+            s.init_explicit()
+            s.run()
+            s.sync()
+            runs.append((s.seismograms(), [s.u(r) for r in range(12)],
+                         [s.sample_points(grid["points"], grid["elem"], rhs=r) for r in range(12)]))
+    assert np.abs(runs[0][2][11]).max() > 0
+    for g, u, f in runs[1:]:
+        assert np.array_equal(g, runs[0][0])
+        for r in range(12):
+            assert np.array_equal(u[r], runs[0][1][r]), r
+            assert np.array_equal(f[r], runs[0][2][r]), r
+    for r in (0, 11):
+        o = oracle.run(m, rhs=r, nthreads=NT)
+        assert np.abs(o["seis"]).max() > 0.1
+        assert per_receiver_rel(runs[0][0][r], o["seis"]).max() <= TOL, r
+
+
 EIGHT_WAVES = [("WAVEP", 0.0), ("WAVEP", 20.0), ("WAVEP", 40.0), ("WAVEP", 60.0),
                ("WAVESV", 0.0), ("WAVESV", 10.0), ("WAVESV", 20.0), ("WAVESV", 25.0)]
 
