@@ -1314,7 +1314,10 @@ int f32_alloc(Ctx &c) {
         const unsigned long long drm = (unsigned long long)std::max(m.ns, 1) * 8 * P.R;
         c.idx32 = c.opts.index_bits != 64 && threads < lim && state < lim && drm < lim;
     }
-    if (c.opts.block_threads <= 0) c.block_threads = 256;
+    // default block: 256, and 128 for the direct gather from four RHS
+    // (measured on 0.1M- and 0.55M-element valleys: 1-3% faster than 256 on
+    // the larger mesh, within 2% either way on the smaller)
+    if (c.opts.block_threads <= 0) c.block_threads = (P.R >= 4 && c.opts.variant == 0) ? 128 : 256;
     // shared-memory tiles (variant 1; variant 0, the default, is the direct gather)
     c.use_tiles = false;
     if (c.opts.variant == 1) {
