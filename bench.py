@@ -220,6 +220,15 @@ def serving_leg(args, local):
     return summary
 
 
+def burst_stream(n):
+    """The saturated serving burst: n decks sized like the serving config
+    (canyons and valleys of 3e4-9e5 elements, 1-16 angles, 1000-2000 steps),
+    as (arrival, problem.in text, steps)."""
+    from exfem import decks
+    return list(decks.serving_stream(n=n, rate=1e9, seed=5, min_scale=0.3, max_scale=1.0, max_angles=16,
+                                     step_range=(1000, 2000), canyon_nperlen=25.0, valley_chper=0.07))
+
+
 def saturated_serving_leg(args, local):
     """Server capacity: a burst of requests sized like the serving config
     (canyons and valleys of 3e4-9e5 elements, 1-16 angles) submitted at once,
@@ -228,13 +237,10 @@ def saturated_serving_leg(args, local):
     admission and stepping included).  The plain FP64 GPU form is timed on
     every request (CUDA events over 10 steps after 3) and its throughput is
     the same total work over the sum of steps x ms/step."""
-    from exfem import decks
     from exfem.gpu import Solver
     from exfem.model import Model
     from exfem.serve import Server
-    stream = decks.serving_stream(n=args.serve_burst, rate=1e9, seed=5, min_scale=0.3, max_scale=1.0,
-                                  max_angles=16, step_range=(1000, 2000), canyon_nperlen=25.0, valley_chper=0.07)
-    reqs = [(Model(d, nsteps=n), n) for _, d, n in stream]
+    reqs = [(Model(d, nsteps=n), n) for _, d, n in burst_stream(args.serve_burst)]
     work = sum(m.nelems * m.problem.nrhs * n for m, n in reqs)
     with Server(max_active=16, chunk_steps=256, device=local) as srv:
         ids = [srv.submit(m, n) for m, n in reqs]
@@ -376,7 +382,14 @@ def run_ours(args, ws, rank, local, dist, torch):
     form = FORMS[args.form]
     fp64 = form == 0
     total = args.warmup + args.steps
-    m = workloads.build(args.workload, scale=args.scale, steps=max(total, 8))
+    if args.burst_request >= 0:
+        # one request of the saturated serving burst, timed alone
+        from exfem.model import Model
+        m = Model(burst_stream(args.serve_burst)[args.burst_request][1], nsteps=max(total, 8))
+        args.workload = "burst request %d of %d" % (args.burst_request, args.serve_burst)
+        args.no_extras = True
+    else:
+        m = workloads.build(args.workload, scale=args.scale, steps=max(total, 8))
     R = m.problem.nrhs
     tuned = {}
     if args.block or args.rpt or args.variant >= 0:
@@ -517,6 +530,8 @@ def main():
                          "pipeline; FP64: 0 reference order, 1 closed form)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--serve-burst", type=int, default=16, help="requests in the saturated serving sample (0: skip)")
+    ap.add_argument("--burst-request", type=int, default=-1,
+                    help="time request I of the saturated serving burst alone (timed loop only)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     ap.add_argument("--accuracy-steps", type=int, default=20000,
                     help="steps of the FP32-vs-FP64 seismogram comparison on the valley (0: skip)")
