@@ -63,6 +63,15 @@ int probe_calck_check(double m, double l) {
 // Threads the plan builder's parallel loops use from here on.
 void probe_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
 
+// The state offset of (node n, dof d, rhs r) for R right-hand sides in
+// groups of lg (row_off / state_at).
+long long probe_state_at(int R, int lg, long long n, int d, int r) {
+    DevModel m{};
+    m.R = R;
+    m.lg = lg;
+    return (long long)state_at(m, (size_t)n, d, r);
+}
+
 void probe_q4_ku(double A, double B, double C, double D, const double *ux, const double *uy, double *fx, double *fy) {
     q4_ku<double>(A, B, C, D, ux, uy, fx, fy);
 }

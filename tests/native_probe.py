@@ -54,6 +54,8 @@ def lib():
     L.probe_plan.argtypes = [C.POINTER(Mesh), C.POINTER(Problem), C.c_int]
     L.probe_plan_free.argtypes = [C.c_void_p]
     L.probe_set_threads.argtypes = [C.c_int]
+    L.probe_state_at.restype = C.c_longlong
+    L.probe_state_at.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_int, C.c_int]
     L.probe_calck_check.restype = C.c_int
     L.probe_calck_check.argtypes = [C.c_double, C.c_double]
     L.probe_plan_size.restype = C.c_longlong

@@ -19,6 +19,26 @@ def ku(mu, lam):
     return k
 
 
+def test_state_layout_groups():
+    """The FP32 state offsets (row_off / state_at): a node's 2R values are
+    its own contiguous block in any grouping; lg = R is the plain layout
+    (n*2 + d)*R + r; with lg = RPT the x then y values of each thread's RPT
+    right-hand sides are adjacent, starting at n*2R + 2*r0, aligned for one
+    vector of 2 RPT values."""
+    L = npb.lib()
+    for R in (1, 2, 4, 6, 8, 12, 16, 24, 64):
+        for lg in {R} | {k for k in (1, 2, 4) if R % k == 0}:
+            for n in (0, 1, 7, 123456789):
+                offs = [L.probe_state_at(R, lg, n, d, r) for d in (0, 1) for r in range(R)]
+                assert sorted(offs) == list(range(n * 2 * R, (n + 1) * 2 * R)), (R, lg)
+                for r0 in range(0, R, lg):
+                    grp = [L.probe_state_at(R, lg, n, d, r0 + j) for d in (0, 1) for j in range(lg)]
+                    assert grp == list(range(n * 2 * R + 2 * r0, n * 2 * R + 2 * r0 + 2 * lg)), (R, lg, r0)
+                    assert (n * 2 * R + 2 * r0) % (2 * lg) == 0
+                if lg == R:
+                    assert offs == [(n * 2 + d) * R + r for d in (0, 1) for r in range(R)]
+
+
 def test_calck_rebuilt_from_six_values_is_bitwise():
     """The FP64 kernels rebuild calck's 8x8 matrix from six per-element values
     computed on the host; every entry must carry the formula's own bits, for
