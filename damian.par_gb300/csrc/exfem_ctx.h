@@ -144,14 +144,14 @@ inline int spread_blocks(long long items, int per_block) {
 // the copy is most of a node's traffic and the corners come from econn:
 // measured 12% faster with one RHS and, with a node's rows paired, 12% at
 // four (0.55M-element valley); the copy is 1-2% faster from six.
-inline bool f32_term_corners(int R) { return R > 4; }
+constexpr bool f32_term_corners(int R) { return R > 4; }
 
 // FP32 direct gather with several threads per node: whether the state is laid
 // out in groups of one thread's right-hand sides (row_off), so that a thread's
 // x and y values of a node are adjacent and move as one vector.  Measured 9 to
 // 12% faster per step from 6 to 16 RHS on a 0.55M-element valley and on the
 // served requests; no gain at 64.
-inline bool f32_interleave(int R) { return R < 64; }
+constexpr bool f32_interleave(int R) { return R < 64; }
 
 // Device memory of a context: a stream-ordered allocation on its stream from
 // the library's memory pool for the device, which keeps what destroyed

@@ -1443,20 +1443,18 @@ int f32_launch_step(Ctx &c, int par) {
     // rows paired when the state is grouped by the thread's RHS (or a thread
     // holds the whole node)
     const bool pair = m.lg == rpt;
-    if (!m.tcorn) {   // few RHS: corners from econn
+    if (!m.tcorn) {   // few RHS (f32_term_corners): corners from econn
+        // below 64 RHS the direct gather's state is always grouped by the
+        // thread's RHS (f32_alloc), so these rows are always paired
+        static_assert(f32_term_corners(5) && f32_interleave(4), "econn corners only with grouped rows");
+        if (!pair) {
+            c.err = "internal: few-RHS step on the plain layout";
+            return EXFEM_E_STATE;
+        }
         switch (rpt) {
-            case 4:
-                if (pair) step32<4, false, true>(c, nb, T, uh, uhn);
-                else step32<4, false, false>(c, nb, T, uh, uhn);
-                break;
-            case 2:
-                if (pair) step32<2, false, true>(c, nb, T, uh, uhn);
-                else step32<2, false, false>(c, nb, T, uh, uhn);
-                break;
-            default:
-                if (pair) step32<1, false, true>(c, nb, T, uh, uhn);
-                else step32<1, false, false>(c, nb, T, uh, uhn);
-                break;
+            case 4: step32<4, false, true>(c, nb, T, uh, uhn); break;
+            case 2: step32<2, false, true>(c, nb, T, uh, uhn); break;
+            default: step32<1, false, true>(c, nb, T, uh, uhn); break;
         }
     } else {
         switch (rpt) {
