@@ -71,3 +71,23 @@ def test_two_gloo_ranks_share_the_max_time():
     assert sorted(r["rank"] for r in res) == [0, 1]
     assert all(r["backend"] == "gloo" for r in res)
     assert all(r["t"] == 13.0 for r in res)
+
+
+def test_burst_stream_is_the_documented_sample():
+    """The saturated serving burst (and `--burst-request I`) is a fixed,
+    seeded sample: 16 canyon/valley decks of 34K-855K elements, 1-16 angles,
+    1000-2000 steps; requests 12 and 6 are the 13- and 12-RHS ones the
+    served-request profiles cover."""
+    import sys
+    sys.path.insert(0, REPO)
+    import bench
+    from exfem.model import Model
+    stream = bench.burst_stream(16)
+    assert len(stream) == 16 and stream == bench.burst_stream(16)
+    models = [Model(d, nsteps=n) for _, d, n in stream]
+    sizes = [m.nelems for m in models]
+    assert min(sizes) == 34368 and max(sizes) == 854616
+    assert all(1 <= m.problem.nrhs <= 16 for m in models)
+    assert all(1000 <= n <= 2000 for _, _, n in stream)
+    assert (models[12].nelems, models[12].problem.nrhs) == (598038, 13)
+    assert (models[6].nelems, models[6].problem.nrhs) == (742906, 12)
