@@ -277,27 +277,46 @@ def saturated_serving_leg(args, local):
                     "fp64 = plain FP64 GPU form, per-request ms/step x steps" % len(reqs)}
 
 
-def accuracy_leg(args, local):
-    """Seismogram error of the FP32 form against the plain FP64 form at full
-    length: the valley mesh with one SV wave (1.5M elements at scale 1, 20000
-    steps), relative L2 and peak amplitude per receiver (the same metrics as
-    the tests, tests/util.py)."""
+def accuracy_leg(args, local, tuned):
+    """Seismogram error of the FP32 form against the plain FP64 form (which
+    matches the oracle to 1e-12), relative L2 and peak amplitude per receiver
+    (the metrics of tests/util.py):
+      - the timed workload itself, the 64-RHS valley, every RHS over
+        `accuracy_batched_steps` steps with the bench's tuned shapes;
+      - the valley with one SV wave at full length (20000 steps)."""
     from exfem import workloads
     from exfem.gpu import Solver
     sys.path.insert(0, os.path.join(HERE, "tests"))
     from util import peak_rel, per_receiver_rel
-    m = workloads.build("valley", scale=args.scale, steps=args.accuracy_steps)
-    seis = {}
-    for prec in (1, 0):
-        with Solver(m, precision=prec, device=local) as s:
-            s.init_explicit()
-            s.run()
-            s.sync()
-            seis[prec] = s.seismograms()
-    return {"workload": "valley", "elements": m.nelems, "rhs": m.problem.nrhs, "steps": m.problem.nsteps,
+
+    def pair(m, kw32):
+        seis = {}
+        for prec in (1, 0):
+            with Solver(m, precision=prec, device=local, **(kw32 if prec == 1 else {})) as s:
+                s.init_explicit()
+                s.run()
+                s.sync()
+                seis[prec] = s.seismograms()
+        return seis
+
+    out = {"against": "plain FP64 GPU form (matches the oracle to 1e-12)", "tolerance": 1e-4}
+    if args.accuracy_batched_steps > 0:
+        mb = workloads.build(args.workload, scale=args.scale, steps=args.accuracy_batched_steps)
+        seis = pair(mb, tuned)
+        l2 = [float(per_receiver_rel(seis[1][r], seis[0][r]).max()) for r in range(mb.problem.nrhs)]
+        pk = [float(peak_rel(seis[1][r], seis[0][r]).max()) for r in range(mb.problem.nrhs)]
+        out.update({"workload": args.workload, "elements": mb.nelems, "rhs": mb.problem.nrhs,
+                    "steps": mb.problem.nsteps, "max_rel_l2": max(l2), "median_rel_l2": float(np.median(l2)),
+                    "max_peak_rel": max(pk), "per_rhs_rel_l2": [round(v, 10) for v in l2],
+                    "worst_rhs": int(np.argmax(l2))})
+    if args.accuracy_steps > 0:
+        m = workloads.build("valley", scale=args.scale, steps=args.accuracy_steps)
+        seis = pair(m, {})
+        out["valley_full_length"] = {
+            "workload": "valley", "elements": m.nelems, "rhs": m.problem.nrhs, "steps": m.problem.nsteps,
             "max_rel_l2": float(per_receiver_rel(seis[1][0], seis[0][0]).max()),
-            "max_peak_rel": float(peak_rel(seis[1][0], seis[0][0]).max()),
-            "against": "plain FP64 GPU form (matches the oracle to 1e-12)", "tolerance": 1e-4}
+            "max_peak_rel": float(peak_rel(seis[1][0], seis[0][0]).max())}
+    return out
 
 
 def config4_leg(args, local):
@@ -345,11 +364,25 @@ def config4_leg(args, local):
     return summary
 
 
+def reference_model(workload, scale, steps):
+    """The workload's mesh and problem as plain arrays: meshed by a child
+    process (which maps the host library) and loaded here, so the process the
+    reference arm times maps the oracle alone."""
+    from oracle.model_arrays import ArrayModel
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "model.npz")
+        code = ("import sys; sys.path[:0] = [%r, %r]; from exfem import workloads; "
+                "from oracle import model_arrays; "
+                "model_arrays.dump(workloads.build(%r, scale=%r, steps=%d), %r)"
+                % (HERE, os.path.join(HERE, "damian.par_gb300"), workload, float(scale), int(steps), path))
+        subprocess.run([sys.executable, "-c", code], check=True)
+        return ArrayModel(path)
+
+
 def run_reference(args, ws, rank, dist):
     if rank != 0:
         return
-    from exfem import workloads
-    m = workloads.build(args.workload, scale=args.scale, steps=20000)
+    m = reference_model(args.workload, args.scale, 20000)
     from oracle import oracle
     nt = os.cpu_count() or 1
     probe = oracle.run(m, nsteps=2, nthreads=nt, want_u=False)["seconds"] / 2.0
@@ -468,10 +501,12 @@ def run_ours(args, ws, rank, local, dist, torch):
         t_req.append(time.perf_counter() - t0)
     t_e2e = sorted(t_req)[1]
     e2e = {"value": ws * me.nelems * R * e2e_steps / t_e2e, "unit": "elem-steps*rhs/s",
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "input_bytes": input_bytes(me),
+           "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
+           "h2d_bytes_per_request": h2d, "d2h_bytes_per_request": d2h, "input_bytes": input_bytes(me),
            "seismogram_bytes": int(seis.nbytes), "request_s": [round(t, 4) for t in t_req],
-           "note": "one request per bench step: create (host plan + uploads) + init_explicit + %d steps + "
-                   "seismograms, median of 3; byte counts are the context's own host<->device copies" % e2e_steps}
+           "note": "a request of %d time steps: create (host plan + uploads) + init_explicit + the steps + "
+                   "seismograms, median of 3; byte counts are the context's own host<->device copies, per "
+                   "request and divided by its time steps" % e2e_steps}
 
     # the plain FP64 form on the same workload, for the FP32 / FP64 ratio
     fp64_ref = None
@@ -491,9 +526,13 @@ def run_ours(args, ws, rank, local, dist, torch):
         del mf
 
     serving = serving_leg(args, local) if args.serve_requests > 0 else None
-    accuracy = accuracy_leg(args, local) if (not fp64 and args.accuracy_steps > 0 and rank == 0) else None
+    accuracy = (accuracy_leg(args, local, tuned)
+                if (not fp64 and (args.accuracy_steps > 0 or args.accuracy_batched_steps > 0) and rank == 0)
+                else None)
     if serving is not None and args.serve_burst > 0:
         serving["saturated"] = saturated_serving_leg(args, local)
+    if serving is not None and args.config4_requests > 0:
+        serving["config4"] = config4_leg(args, local)
 
     if rank != 0:
         return
@@ -534,10 +573,13 @@ def main():
                     help="time request I of the saturated serving burst alone (timed loop only)")
     ap.add_argument("--fp64-steps", type=int, default=10, help="steps of the plain FP64 form timed for comparison")
     ap.add_argument("--accuracy-steps", type=int, default=20000,
-                    help="steps of the FP32-vs-FP64 seismogram comparison on the valley (0: skip)")
+                    help="steps of the FP32-vs-FP64 seismogram comparison on the one-wave valley (0: skip)")
+    ap.add_argument("--accuracy-batched-steps", type=int, default=2000,
+                    help="steps of the FP32-vs-FP64 comparison of every RHS of the timed workload (0: skip)")
     ap.add_argument("--serve-config4", action="store_true",
                     help="only the serving config as specified (512 requests, minutes of GPU time); prints its own line")
-    ap.add_argument("--config4-requests", type=int, default=512)
+    ap.add_argument("--config4-requests", type=int, default=512,
+                    help="requests of the serving config run inside the default line (serving.config4; 0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

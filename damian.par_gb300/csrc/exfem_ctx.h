@@ -174,6 +174,7 @@ int f64_launch_hang(Ctx &c, double *unew, int mode);
 // Launchers implemented by the FP32 file.
 int f32_alloc(Ctx &c);
 int f32_init(Ctx &c);
+int f32_tune_in_place(Ctx &c);
 int f32_launch_step(Ctx &c, int par);
 int f32_launch_sample0(Ctx &c, int par);
 // bf16 <-> float on the host (round to nearest even), for tests and read-back.

@@ -680,11 +680,16 @@ struct PipeArgs {
     int tn, ntiles, nstage;
     unsigned stage_bytes;   // one stage; regions at the offsets below
     unsigned off_dh, off_dc, off_uc, off_nrec, off_ts, off_tk;
+    long long wait_cycles;  // bound of each pipeline wait (exfem_opts.wait_cycles)
 };
 
 constexpr int PIPE_RUNS = 64;
 constexpr int PIPE_MAX_STAGES = 4;
-constexpr long long PIPE_WAIT_CYCLES = 2000000000LL;   // about 1 s at 2 GHz
+constexpr long long PIPE_WAIT_CYCLES = 2000000000LL;   // default bound: about 1 s at 2 GHz
+// Bounds below this poll with mbarrier.test_wait, which returns at once;
+// longer ones use try_wait, which may suspend the thread for a while (and so
+// could outlast a short bound on its own).
+constexpr long long PIPE_POLL_BELOW = 1000000LL;
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -700,12 +705,26 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
     return ok != 0;
 }
 
-// Waits for the phase with the given parity to complete; false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_test_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity to complete, for at most
+// `budget` SM cycles (and 2^26 polls); false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity, long long budget) {
     const long long t0 = clock64();
+    const bool poll = budget < PIPE_POLL_BELOW;
     for (int it = 0; it < (1 << 26); ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (clock64() - t0 > PIPE_WAIT_CYCLES) break;
+        if (poll ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity)) return true;
+        if (clock64() - t0 > budget) break;
     }
     return false;
 }
@@ -754,7 +773,7 @@ __device__ __forceinline__ void pipe_produce(const DevModel &m, const PipeArgs &
         }
         const int s = k % NS;
         if (k >= NS) {
-            const bool w = mbar_wait_bounded(smem_addr(empty + s), (unsigned)(k / NS - 1) & 1u);
+            const bool w = mbar_wait_bounded(smem_addr(empty + s), (unsigned)(k / NS - 1) & 1u, pa.wait_cycles);
             if (!__all_sync(0xffffffffu, w)) { ok = false; break; }
             // the consumers' reads of the stage (generic proxy) come before the refill (async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -785,13 +804,15 @@ __device__ __forceinline__ void pipe_produce(const DevModel &m, const PipeArgs &
         ra = ra2;
         rb = rb2;
     }
-    if (!ok) {
-        if (lane == 0) {
-            atomicOr(m.d_flag, 2);
-            for (int j = max(0, k - NS); j < k; ++j)   // copies that may still be in flight
-                mbar_wait_bounded(smem_addr(full + j % NS), (unsigned)(j / NS) & 1u);
-        }
-    }
+    if (!ok && lane == 0) atomicOr(m.d_flag, 2);
+    // Copies that may still be in flight (the last NS tiles issued): the
+    // producer leaves only once they have landed, so no copy outlives the
+    // block even when the consumers gave up early.  Always the default bound:
+    // a short caller bound must not cut this wait.
+    if (lane == 0)
+        for (int j = max(0, k - NS); j < k; ++j)
+            mbar_wait_bounded(smem_addr(full + j % NS), (unsigned)(j / NS) & 1u, PIPE_WAIT_CYCLES);
+    __syncwarp();
 }
 
 template <int RPT>
@@ -825,7 +846,7 @@ __global__ void __launch_bounds__(544) k_pipe32(DevModel m, PipeArgs pa, const f
     int k = 0;
     for (int t = blockIdx.x; t < pa.ntiles; t += gridDim.x, ++k) {
         const int s = k % NS;
-        const bool w = mbar_wait_bounded(smem_addr(full + s), (unsigned)(k / NS) & 1u);
+        const bool w = mbar_wait_bounded(smem_addr(full + s), (unsigned)(k / NS) & 1u, pa.wait_cycles);
         if (!__all_sync(0xffffffffu, w)) {
             if (lane == 0) atomicOr(m.d_flag, 2);
             return;
@@ -1380,6 +1401,66 @@ int f32_alloc(Ctx &c) {
     return EXFEM_OK;
 }
 
+// The direct gather's shape: right-hand sides per thread and block size,
+// with what depends on them (the state's RHS grouping and the index width).
+static void f32_set_shape(Ctx &c, int rpt, int block) {
+    const Plan &P = c.plan;
+    c.rhs_per_thread = rpt;
+    c.block_threads = block;
+    c.dm.lg = (rpt < P.R && f32_interleave(P.R)) ? rpt : P.R;
+    const unsigned long long lim = 1ull << 32;
+    const unsigned long long threads = (unsigned long long)P.n_active * (P.R / rpt) + 1024;
+    const unsigned long long state = (unsigned long long)P.nn * 2 * P.R;
+    const unsigned long long drm = (unsigned long long)std::max(c.dm.ns, 1) * 8 * P.R;
+    c.idx32 = c.opts.index_bits != 64 && threads < lim && state < lim && drm < lim;
+}
+
+// exfem_opts.tune: before the state is set up, time every shape of the
+// direct gather (RHS per thread 1, 2, 4 dividing R; blocks of 128, 256, 512)
+// on the context itself for a few steps from the zero state, and keep the
+// fastest.  The steps run from step 1 again for every shape (device counter
+// reset), at most min(nsteps, 4) of them, so the receiver slots they write
+// stay inside the seismogram buffer; init_explicit then clears it all.
+int f32_tune_in_place(Ctx &c) {
+    if (c.use_tiles || c.use_pipe || c.opts.rhs_per_thread > 0 || c.opts.block_threads > 0) return EXFEM_OK;
+    const int nst = std::min(c.plan.nsteps, 4);
+    if (nst < 2) return EXFEM_OK;
+    cudaEvent_t a = nullptr, b = nullptr;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    int best_rpt = c.rhs_per_thread, best_bt = c.block_threads, rc = EXFEM_OK;
+    float best = -1.f;
+    for (int rpt : {1, 2, 4}) {
+        if (c.plan.R % rpt) continue;
+        for (int bt : {128, 256, 512}) {
+            f32_set_shape(c, rpt, bt);
+            if ((rc = f32_init(c))) break;
+            if (cudaMemsetAsync(c.dm.d_step, 0, 4 * sizeof(int), c.stream) != cudaSuccess) { rc = EXFEM_E_CUDA; break; }
+            int par = 0;
+            if ((rc = f32_launch_step(c, par))) break;   // warm-up step
+            par ^= 1;
+            cudaEventRecord(a, c.stream);
+            for (int i = 1; i < nst && rc == EXFEM_OK; ++i) {
+                rc = f32_launch_step(c, par);
+                par ^= 1;
+            }
+            cudaEventRecord(b, c.stream);
+            float ms = 0.f;
+            if (rc || cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+                if (!rc) rc = EXFEM_E_CUDA;
+                break;
+            }
+            if (best < 0.f || ms < best) { best = ms; best_rpt = rpt; best_bt = bt; }
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) { if (c.err.empty()) c.err = "shape tuning failed"; return rc; }
+    f32_set_shape(c, best_rpt, best_bt);
+    return EXFEM_OK;
+}
+
 int f32_init(Ctx &c) {
     size_t nst = (size_t)c.plan.nn * 2 * c.plan.R;
     CK(cudaMemsetAsync(c.uhi[0], 0, nst * sizeof(float), c.stream));
@@ -1418,7 +1499,8 @@ int f32_launch_step(Ctx &c, int par) {
         PipeArgs pa{static_cast<const int4 *>(c.p_hdr), static_cast<const int2 *>(c.p_runs),
                     static_cast<const int4 *>(c.p_nrec), static_cast<const int4 *>(c.p_tpack), c.t_lslot,
                     c.tile_tn, c.tile_n, c.pipe_nstage, c.pipe_stage,
-                    c.pipe_off[0], c.pipe_off[1], c.pipe_off[2], c.pipe_off[3], c.pipe_off[4], c.pipe_off[5]};
+                    c.pipe_off[0], c.pipe_off[1], c.pipe_off[2], c.pipe_off[3], c.pipe_off[4], c.pipe_off[5],
+                    c.opts.wait_cycles > 0 ? (long long)c.opts.wait_cycles : PIPE_WAIT_CYCLES};
         const int threads = c.pipe_threads;
         switch (rpt) {
             case 4: k_pipe32<4><<<c.pipe_grid, threads, c.tile_smem, c.stream>>>(m, pa, uh, uhn, c.ucomp, c.udel[0], c.dcomp); break;

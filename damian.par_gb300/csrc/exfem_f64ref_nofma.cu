@@ -390,27 +390,49 @@ __global__ void k_noalloc_prep(int *counters, int step) {
 
 }  // namespace exfem
 
+namespace {
+
+// Puts the caller's current device back when the entry point returns.
+struct DeviceRestore {
+    int prev = -1;
+    ~DeviceRestore() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
 extern "C" int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const double *d_um,
-                                      double *d_unew) {
+                                      double *d_unew, void *stream) {
     using namespace exfem;
     if (!ctx || !d_u || !d_um || !d_unew) return EXFEM_E_ARG;
     Ctx &c = *ctx;
     if (c.precision != EXFEM_FP64) { c.err = "exfem_gpu_step_noalloc needs an EXFEM_FP64 context"; return EXFEM_E_ARG; }
+    if (c.opts.variant != EXFEM_VARIANT_REFERENCE_ORDER) {
+        c.err = "exfem_gpu_step_noalloc runs the reference-order kernels only: create the context with "
+                "variant = EXFEM_VARIANT_REFERENCE_ORDER";
+        return EXFEM_E_ARG;
+    }
     if (step < 1) { c.err = "step must be >= 1 (the time index i of explicit.f90:125)"; return EXFEM_E_ARG; }
+    if (c.device < 0 || c.device >= 128) { c.err = "device ordinal out of range"; return EXFEM_E_ARG; }
     const Plan &P = c.plan;
     const size_t ns = P.s_elem.size();
+    // 32 head doubles, the DRM forces rounded up to 4 doubles (the element
+    // forces' double4 stores stay 32-byte aligned), then the element forces
     const size_t ef_off = kNoallocHeadDoubles + ((ns * 16 * (size_t)P.R + 3) & ~(size_t)3);
     const size_t need = ef_off + (size_t)P.ne * 8 * P.R;
     if (need > kNoallocScratchDoubles) {
         c.err = "exfem_gpu_step_noalloc: the model needs " + std::to_string(need) +
-                " doubles of scratch (8 per element and right-hand side, 16 per DRM element and right-hand side, "
-                "plus 32); the static limit is EXFEM_NOALLOC_SCRATCH_DOUBLES = " +
-                std::to_string(kNoallocScratchDoubles);
+                " doubles of scratch (32 + 16*nseismic*nrhs rounded up to a multiple of 4 + 8*nelems*nrhs); "
+                "the static limit is EXFEM_NOALLOC_SCRATCH_DOUBLES = " + std::to_string(kNoallocScratchDoubles);
         return EXFEM_E_ARG;
     }
-    cudaError_t e = cudaSetDevice(c.device);
+    DeviceRestore restore;
+    cudaError_t e = cudaGetDevice(&restore.prev);
+    if (e != cudaSuccess) { restore.prev = -1; c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
+    if (restore.prev == c.device) restore.prev = -1;   // nothing to put back
+    e = cudaSetDevice(c.device);
     if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
-    if (c.device < 0 || c.device >= 128) { c.err = "device ordinal out of range"; return EXFEM_E_ARG; }
     double *base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_noalloc_mu);
@@ -425,25 +447,26 @@ extern "C" int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_
         }
         base = g_noalloc_addr[c.device];
     }
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : c.stream;
     DevModel m = c.dm;
     int *counters = reinterpret_cast<int *>(base);
     m.d_step = counters;
     m.d_flag = counters + 1;
     m.d_blocks = reinterpret_cast<unsigned *>(counters + 2);
     m.fdrm = base + kNoallocHeadDoubles;
-    m.nrecv = 0;   // receivers stay with exfem_gpu_run
+    m.nrecv = 0;   // receivers (and with them the NaN watchdog) stay with exfem_gpu_run
     double *ef = base + ef_off;
     const int T = 128;
-    k_noalloc_prep<<<1, 1, 0, c.stream>>>(counters, step);
+    k_noalloc_prep<<<1, 1, 0, st>>>(counters, step);
     if (m.ns > 0) {
         const long long W = (long long)m.ns * m.R;
         const int ipb = spread_per_block(W, c.num_sms, 8);
-        k_drm_ref<<<spread_blocks(W, ipb), 128, 0, c.stream>>>(m, ipb);
+        k_drm_ref<<<spread_blocks(W, ipb), 128, 0, st>>>(m, ipb);
     }
-    k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, d_u, d_um, ef);
-    k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, ef, d_unew);
+    k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, st>>>(m, d_u, d_um, ef);
+    k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, st>>>(m, ef, d_unew);
     int nbh = (int)std::max<long long>(1, ((long long)m.n_hang * m.R + T - 1) / T);
-    k_hang_ref<<<nbh, T, 0, c.stream>>>(m, d_unew, nbh, 0, 1, 0, 1);
+    k_hang_ref<<<nbh, T, 0, st>>>(m, d_unew, nbh, 0, 1, 0, 1);
     e = cudaGetLastError();
     if (e != cudaSuccess) { c.err = cudaGetErrorString(e); return EXFEM_E_CUDA; }
     c.launches += 4 + (m.ns > 0 ? 1 : 0);

@@ -548,6 +548,8 @@ void exfem_gpu_default_opts(exfem_opts *o) {
     o->variant = EXFEM_VARIANT_REFERENCE_ORDER;
     o->index_bits = 0;
     o->pad_rhs = 0;
+    o->wait_cycles = 0;
+    o->tune = 0;
 }
 
 int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts, exfem_ctx **out) {
@@ -564,6 +566,8 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     }
     if (o.index_bits != 0 && o.index_bits != 64) { g_create_err = "index_bits must be 0 or 64"; return EXFEM_E_ARG; }
     if (o.pad_rhs != 0 && o.pad_rhs != 1) { g_create_err = "pad_rhs must be 0 or 1"; return EXFEM_E_ARG; }
+    if (o.wait_cycles < 0) { g_create_err = "wait_cycles must be >= 0"; return EXFEM_E_ARG; }
+    if (o.tune != 0 && o.tune != 1) { g_create_err = "tune must be 0 or 1"; return EXFEM_E_ARG; }
     const int max_bt = o.precision == EXFEM_FP64 ? 256 : 512;   // the kernels' __launch_bounds__
     if (o.block_threads < 0 || o.block_threads > max_bt || (o.block_threads % 32) != 0) {
         g_create_err = "block_threads must be a multiple of 32 in [0, " + std::to_string(max_bt) + "]";
@@ -618,7 +622,8 @@ int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out) {
             CK(cudaGetLastError());
         }
     } else {
-        int rc = f32_init(c);
+        int rc = c.opts.tune ? f32_tune_in_place(c) : EXFEM_OK;
+        if (!rc) rc = f32_init(c);
         if (rc) return rc;
     }
     CK(cudaMemsetAsync(m.seis, 0, sizeof(double) * (size_t)c.plan.R * c.plan.nsave * std::max(c.plan.nrecv, 1) * 2,
@@ -685,8 +690,9 @@ int exfem_gpu_sync(exfem_ctx *ctx) {
     int flag = 0;
     CK(cudaMemcpy(&flag, c.dm.d_flag, sizeof(int), cudaMemcpyDeviceToHost));
     c.d2h_bytes += sizeof(int);
-    if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
+    // a timed-out wait leaves the state incomplete, so it is reported first
     if (flag & 2) { c.err = "a bounded device wait timed out"; return EXFEM_E_TIMEOUT; }
+    if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
     return EXFEM_OK;
 }
 
@@ -700,6 +706,7 @@ int exfem_gpu_query(exfem_ctx *ctx) {
     int flag = 0;
     CK(cudaMemcpy(&flag, c.dm.d_flag, sizeof(int), cudaMemcpyDeviceToHost));
     c.d2h_bytes += sizeof(int);
+    if (flag & 2) { c.err = "a bounded device wait timed out"; return EXFEM_E_TIMEOUT; }
     if (flag & 1) { c.err = "non-finite receiver sample (the run diverged)"; return EXFEM_E_NAN; }
     return EXFEM_OK;
 }

@@ -529,7 +529,8 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             const double *dv = P.edamp[ie] >= 0 ? &P.edampv[(size_t)P.edamp[ie] * 8] : nullptr;
             for (int d = 0; d < 2; ++d) {
                 double damping = dv ? dv[2 * k + d] : 0.0;
-                acc[d] = acc[d] + (P.a2 * damping + P.a1 * mass);
+                // e_mfull(dofs) + e_a(2)*damping + e_a(1)*mass, left to right
+                acc[d] = (acc[d] + P.a2 * damping) + P.a1 * mass;
             }
         }
         P.mfull_ref[2 * x] = acc[0];
@@ -806,6 +807,40 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
         for (int x : nodes) slot[x] = -1;
     }
     return EXFEM_OK;
+}
+
+bool build_mma_tiles(const Plan &P, int tn, int emax_limit, MmaTiles &T, std::string &why) {
+    T = MmaTiles();
+    if (tn < 1 || emax_limit < 1 || emax_limit > 255) { why = "bad tile shape"; return false; }
+    T.tn = tn;
+    T.ntiles = (P.n_active + tn - 1) / tn;
+    T.eptr.assign(T.ntiles + 1, 0);
+    T.tj.assign(P.tlist.size(), 0);
+    std::vector<int> local(P.ne, -1), elems;
+    for (int t = 0; t < T.ntiles; ++t) {
+        const int n0 = t * tn, n1 = std::min(P.n_active, n0 + tn);
+        elems.clear();
+        for (int n = n0; n < n1; ++n)
+            for (int q = P.tptr[n]; q < P.tptr[n + 1]; ++q) {
+                const int e = (P.tlist[q] >> 1) >> 2;
+                if (local[e] < 0) {
+                    local[e] = (int)elems.size();
+                    elems.push_back(e);
+                }
+                T.tj[q] = (unsigned char)std::min(local[e], 255);
+            }
+        if ((int)elems.size() > emax_limit) {
+            why = "tile " + std::to_string(t) + " reads " + std::to_string(elems.size()) + " elements (limit " +
+                  std::to_string(emax_limit) + ")";
+            for (int e : elems) local[e] = -1;
+            return false;
+        }
+        T.emax = std::max(T.emax, (int)elems.size());
+        T.elist.insert(T.elist.end(), elems.begin(), elems.end());
+        T.eptr[t + 1] = (int)T.elist.size();
+        for (int e : elems) local[e] = -1;
+    }
+    return true;
 }
 
 pvec<float> node_coef32(const Plan &P) {

@@ -72,7 +72,8 @@ class Opts(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("use_graph", C.c_int),
                 ("graph_steps", C.c_int), ("block_threads", C.c_int),
                 ("rhs_per_thread", C.c_int), ("reorder", C.c_int), ("check_every", C.c_int),
-                ("variant", C.c_int), ("index_bits", C.c_int), ("pad_rhs", C.c_int)]
+                ("variant", C.c_int), ("index_bits", C.c_int), ("pad_rhs", C.c_int),
+                ("wait_cycles", C.c_int), ("tune", C.c_int)]
 
 
 class ModelInfo(C.Structure):
@@ -129,7 +130,9 @@ GPU_SYMBOLS = {
     "exfem_gpu_run_timed": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "exfem_gpu_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
                                             C.POINTER(C.c_char_p), C.c_int]),
-    "exfem_gpu_step_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "exfem_gpu_autotune": (C.c_int, [C.POINTER(Mesh), C.POINTER(Problem), C.POINTER(Opts), C.c_int,
+                                     C.POINTER(C.c_double)]),
+    "exfem_gpu_step_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "exfem_gpu_steps_done": (C.c_int, [C.c_void_p]),
     "exfem_gpu_launch_count": (C.c_longlong, [C.c_void_p]),
     "exfem_gpu_device_bytes": (C.c_size_t, [C.c_void_p]),

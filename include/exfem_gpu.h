@@ -143,6 +143,22 @@ typedef struct exfem_opts {
                           waves when that aligns the state rows; 1 = never.
                           Same results; every output covers only the caller's
                           right-hand sides                                    */
+    int wait_cycles;   /* bound of each device-side wait (the mbarrier waits
+                          of FP32 variant 2), in SM clock cycles; 0 = the
+                          library default, 2e9 (about 1 s at 2 GHz).  A wait
+                          that runs out sets a watchdog flag; the kernel then
+                          waits (with the default bound) for its own copies
+                          in flight and returns, and exfem_gpu_sync reports
+                          EXFEM_E_TIMEOUT.  The counterpart of the
+                          reference's fatal mpi_abort path
+                          (communicator.f90:144-156), as a status          */
+    int tune;          /* FP32 direct gather: 1 = at exfem_gpu_init_explicit,
+                          time every right-hand-sides-per-thread and block
+                          shape on this context for a few steps from rest
+                          (CUDA events on its stream) and keep the fastest,
+                          unless rhs_per_thread or block_threads is set; the
+                          state is then reset.  0 = the built-in choice.
+                          Same results either way                         */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;
@@ -218,24 +234,54 @@ int exfem_gpu_profile_kernels(exfem_ctx *ctx, int nsteps, double *ms_out, const 
 /* One FP64 time step on buffers the caller owns, with no device allocation.
  * No counterpart in the reference.
  *
- * For callers that keep the displacement state in device memory they manage
- * themselves and may not call cudaMalloc or cudaFree while stepping: a host
- * that captures its own time loop into a CUDA graph (allocation is not
- * permitted while a stream is being captured) or a host whose own pool owns
- * every device byte.  cudaFree would also synchronize the whole device.
+ * For hosts that keep the displacement state in device memory they manage
+ * themselves and cannot let a library allocate: a host whose own pool or
+ * arena hands out every device byte up front (a cudaMalloc from the library
+ * would fall outside its budget, or fail once the arena holds the memory),
+ * or a host with other work in flight on the device, which cudaFree would
+ * stall, since cudaFree synchronizes the whole device.
  *
  * d_u, d_um: device arrays of u_i and u_{i-1}; d_unew receives u_{i+1}
- * (2*nnodes*nrhs doubles each, the context's internal node order, the layout
- * exfem_gpu_run keeps; d_unew may alias d_um).  `step` is the time index i+1
- * whose forcing is applied (t = step*dt, explicit.f90:128).  Receivers are
- * not sampled.  The element and DRM forces go through one static scratch
- * array shared by every call: the model must fit
- * 32 + 16*nseismic*nrhs + 8*nelems*nrhs <= EXFEM_NOALLOC_SCRATCH_DOUBLES
- * (EXFEM_E_ARG otherwise), and calls that overlap on the GPU (two contexts,
- * two streams) race on it.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  Queued on
- * the context's stream; exfem_gpu_sync() waits for it. */
-int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const double *d_um, double *d_unew);
+ * (2*nnodes*nrhs doubles each, in the context's internal node order, the
+ * layout exfem_gpu_run keeps; d_unew may alias d_um, the two-array rotation
+ * of e_u/e_up).  `step` is the time index i+1 whose forcing is applied
+ * (t = step*dt, explicit.f90:128).  The context must be EXFEM_FP64 with
+ * variant EXFEM_VARIANT_REFERENCE_ORDER (EXFEM_E_ARG otherwise).
+ *
+ * Receivers are not sampled, so the NaN watchdog of exfem_gpu_run does not
+ * run either: a diverging loop gets no EXFEM_E_NAN from this entry point.
+ *
+ * The element and DRM forces go through one static scratch array shared by
+ * every call; the model must fit
+ *   32 + 4*ceil(16*nseismic*nrhs / 4) + 8*nelems*nrhs
+ *     <= EXFEM_NOALLOC_SCRATCH_DOUBLES
+ * (EXFEM_E_ARG with a message otherwise).  The array keeps the last call's
+ * contents; each call resets the counters it reads.  Calls that overlap on
+ * the GPU (two contexts, two streams) race on it.  The first call on a
+ * device looks up the array's device address with that device current.
+ *
+ * stream: the cudaStream_t the five launches are queued on, so they are
+ * ordered after the caller's own writes of d_u/d_um and before its reads of
+ * d_unew.  NULL queues them on the context's own stream, a non-blocking one
+ * that does not wait for the legacy default stream (exfem_gpu_sync() waits
+ * for it); a caller on the legacy default stream passes cudaStreamLegacy.
+ * The caller's current device is the same on return as on entry. */
+int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const double *d_um, double *d_unew,
+                           void *stream);
+
+/* Autotuner of the FP32 form (opts->precision must be EXFEM_FP32_KAHAN).
+ * Times every candidate shape on this mesh and problem and writes the
+ * fastest into opts: variant (0 direct gather, 1 shared-memory tiles, 2
+ * bulk-copy pipeline when the right-hand sides are a multiple of 4),
+ * block_threads (128, 256, 512) and rhs_per_thread (1, 2, 4).  Each
+ * candidate runs in a context of its own (one at a time: the device must
+ * hold one more context of this problem), 3 warm-up steps and `steps` steps
+ * timed with CUDA events (1 <= steps <= 1000); *ms_per_step (nullable)
+ * receives the winner's time.  Results are cached in the process per
+ * (elements, nodes, right-hand sides, device).  No counterpart in the
+ * reference, whose element loop has one shape (explicit.f90:129-142). */
+int exfem_gpu_autotune(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opts *opts, int steps,
+                       double *ms_per_step);
 
 /* Steps taken so far. */
 int exfem_gpu_steps_done(const exfem_ctx *ctx);

@@ -4,7 +4,8 @@
   exfem_oracle.cpp (FP64, -ffp-contract=off so x86 and Arm round alike).
 * ``oracle/_ref/libref_io.so`` — the reference's own ``io.cpp`` (problem.in
   parser and mesh/mass/step/sheet file I/O), compiled unchanged from the
-  read-only reference tree when that tree is present.  It pins the file
+  read-only reference tree (``EXFEM_REFERENCE_TREE``) when that tree is
+  present.  It pins the file
   formats and the deck parser; the solver itself cannot be compiled (Fortran,
   MPI, ParMETIS and ACML are absent, and model.f90:643 does not compile).
 """
@@ -19,7 +20,8 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 ORACLE_LIB = os.path.join(BUILD, "libexfem_oracle.so")
 REF_IO_LIB = os.path.join(REF_OUT, "libref_io.so")
-REFERENCE_TREE = "/root/reference"
+# where the reference's source tree is mounted read-only (absent on GPU hosts)
+REFERENCE_TREE = os.environ.get("EXFEM_REFERENCE_TREE", "/root/reference")
 
 
 def _run(cmd):

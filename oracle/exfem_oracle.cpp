@@ -491,7 +491,8 @@ int oracle_run(const exfem_mesh *mesh, const exfem_problem *prob, int rhs, int h
         S.elemallnhdofs(i, dofs);
         double mass = S.getmassof(i), damping[8];
         S.getdampingof(i, damping);
-        for (int k = 0; k < 8; ++k) S.mfull[dofs[k] - 1] = S.mfull[dofs[k] - 1] + (S.ea[1] * damping[k] + S.ea[0] * mass);
+        // explicit.f90:100-102 adds left to right: (e_mfull + e_a(2)*damping) + e_a(1)*mass
+        for (int k = 0; k < 8; ++k) S.mfull[dofs[k] - 1] = (S.mfull[dofs[k] - 1] + S.ea[1] * damping[k]) + S.ea[0] * mass;
     }
     S.sum_reactanchors(S.mfull);
     if (mfull_out) std::memcpy(mfull_out, S.mfull.data(), sizeof(double) * ndof);

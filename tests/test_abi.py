@@ -56,6 +56,10 @@ def test_argument_errors_need_no_device():
     bad = default_opts(index_bits=32)   # 0 (automatic) or 64
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
     assert b"index_bits" in L.exfem_gpu_last_error(None)
+    assert default_opts().wait_cycles == 0       # the library's default bound
+    bad = default_opts(wait_cycles=-1)
+    assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
+    assert b"wait_cycles" in L.exfem_gpu_last_error(None)
 
 
 def test_estimate_counts_rhs_padding():

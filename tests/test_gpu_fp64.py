@@ -15,7 +15,7 @@ from exfem.abi import (EXFEM_E_ARG, EXFEM_E_STATE, EXFEM_E_UNSUPPORTED, EXFEM_VA
 from exfem.gpu import Solver
 from exfem.model import Model
 from oracle import oracle
-from util import per_receiver_rel, rel
+from util import fp64_rel, per_receiver_rel, rel
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
@@ -38,7 +38,7 @@ def test_rectangle_matches_oracle():
     g = gpu_run(m)
     assert np.array_equal(g["mfull"], o["mfull"])
     assert np.abs(o["seis"]).max() > 1.0
-    err = per_receiver_rel(g["seis"][0], o["seis"])
+    err = fp64_rel(g["seis"][0], o["seis"])
     assert err.max() <= TOL, err.max()
     assert rel(g["u"][0], o["u"]) <= TOL
     assert g["launches"] > 0
@@ -51,7 +51,7 @@ def test_canyon_with_hanging_nodes_every_rhs():
     for r in range(m.problem.nrhs):
         o = oracle.run(m, rhs=r, nthreads=NT)
         assert np.array_equal(g["mfull"], o["mfull"])
-        err = per_receiver_rel(g["seis"][r], o["seis"])
+        err = fp64_rel(g["seis"][r], o["seis"])
         assert err.max() <= TOL, (r, err.max())
         assert rel(g["u"][r], o["u"]) <= TOL
 
@@ -60,14 +60,14 @@ def test_valley_heterogeneous():
     m = workloads.build("valley", scale=0.12, steps=300, save_every=3)
     o = oracle.run(m, nthreads=NT)
     g = gpu_run(m)
-    assert per_receiver_rel(g["seis"][0], o["seis"]).max() <= TOL
+    assert fp64_rel(g["seis"][0], o["seis"]).max() <= TOL
 
 
 def test_closed_form_variant():
     m = workloads.build("canyon", scale=0.15, steps=400, refine_band=20)
     o = oracle.run(m, rhs=4, nthreads=NT)
     g = gpu_run(m, variant=EXFEM_VARIANT_CLOSED_FORM)
-    assert per_receiver_rel(g["seis"][4], o["seis"]).max() <= 1e-10
+    assert fp64_rel(g["seis"][4], o["seis"]).max() <= 1e-10
 
 
 def test_graph_chunks_and_numbering_do_not_change_results():
@@ -89,7 +89,7 @@ def test_full_size_homogeneous_rectangle():
     m = workloads.build("homogeneous_rectangle")
     o = oracle.run(m, nthreads=NT)
     g = gpu_run(m)
-    err = per_receiver_rel(g["seis"][0], o["seis"])
+    err = fp64_rel(g["seis"][0], o["seis"])
     assert err.max() <= TOL, err.max()
 
 

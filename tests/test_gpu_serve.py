@@ -36,9 +36,12 @@ def alone32(m, steps):
         return s.seismograms()[:, : steps // m.problem.io_interval + 1]
 
 
-def test_each_result_is_the_same_in_the_mix_as_alone():
+@pytest.mark.parametrize("tune", [0, 1], ids=["built_in_shapes", "tuned_shapes"])
+def test_each_result_is_the_same_in_the_mix_as_alone(tune):
+    """With tune = 1 every request's context times its own shapes first
+    (exfem_opts.tune): the results are still those of the request alone."""
     reqs = mix()
-    with Server(max_active=4, chunk_steps=64) as srv:
+    with Server(max_active=4, chunk_steps=64, tune=tune) as srv:
         ids = [srv.submit(m, n) for m, n in reqs]
         res = srv.wait_all(len(ids))
         assert len(res) == len(ids) and all(r["status"] == 0 for r in res)
