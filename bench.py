@@ -149,7 +149,7 @@ def kernel_bytes(name, m, R, fp64):
         return ns * (64 + 16 * s * R)
     if name.startswith("k_hang"):
         return nh * 2 * 3 * s * R + nr * (4 * 2 * s * R + 2 * 8 * R)
-    if name.startswith(("k_step32", "k_tile32", "k_pipe32")):
+    if name.startswith(("k_step32", "k_tile32", "k_pipe32", "k_mma32")):
         return 6 * ndof * 4 * R + ne * 32 + 4 * inc
     return None
 

@@ -103,6 +103,13 @@ struct Ctx {
     int p32_n = 0;
     // bulk-copy pipeline of the FP32 step (variant 2): per-tile headers and
     // halo runs, node records, term records; persistent grid
+    // tensor-core step of the FP32 form (variant 3): element tiles and the
+    // split [Kmu; Klambda] operand
+    bool use_mma = false;
+    int mma_ntiles = 0;
+    const int *mma_nptr = nullptr, *mma_eptr = nullptr, *mma_elist = nullptr;
+    const unsigned char *mma_tj = nullptr;
+    const float *mma_btile = nullptr;
     bool use_pipe = false;
     const void *p_hdr = nullptr, *p_runs = nullptr, *p_nrec = nullptr, *p_tpack = nullptr;
     int pipe_grid = 0, pipe_threads = 0, pipe_nstage = 0;

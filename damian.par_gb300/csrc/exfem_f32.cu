@@ -42,6 +42,7 @@
 
 #include "exfem_ctx.h"
 #include "exfem_device.cuh"
+#include "exfem_tc.cuh"
 
 namespace exfem {
 
@@ -330,6 +331,67 @@ __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
     for (int q = 0; q < 3; ++q) out[((size_t)s * 4 + k) * 3 * m.R + (size_t)q * m.R + r] = v[q];
 }
 
+// The rest of a node's step once its DRM and element terms are in (ax, ay):
+// the dashpot term, the hanging nodes it anchors, and the Kahan-compensated
+// increment update of D and u (shared by the direct gather and the
+// tensor-core step).
+template <int RPT, bool PAIR, typename I>
+__device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R, I roff, float (&ax)[RPT],
+                                            float (&ay)[RPT], const float *__restrict__ uh,
+                                            float *__restrict__ uhn, unsigned short *__restrict__ uc,
+                                            float *__restrict__ dh, unsigned short *__restrict__ dc) {
+    // dashpot term -2 a2 C D (zero away from the absorbing boundary)
+    const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
+    float dx[RPT], dy[RPT];
+    XY<RPT, PAIR>::load_cg(dh + bn, R, dx, dy);
+    if (nc.z != 0.f || nc.w != 0.f) {
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
+    }
+    float unx[RPT], uny[RPT];
+    XY<RPT, PAIR>::load(uh + bn, R, unx, uny);
+    // hanging nodes this node anchors:
+    //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_h - u_n) + (D_h - D_n)) ]
+    // (u_h, D_h from the hanging node's rows, which change only in k_hang32;
+    // the other anchor's row is rewritten in place during this kernel)
+    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
+        int h = __ldg(m.llist + 2 * q);
+        float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
+        I bh = ((I)h * 2) * R + roff;
+        float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
+        XY<RPT, PAIR>::load_cg(dh + bh, R, hx, hy);
+        XY<RPT, PAIR>::load(uh + bh, R, uhx, uhy);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * ((uhx[j] - unx[j]) + (hx[j] - dx[j])));
+            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * ((uhy[j] - uny[j]) + (hy[j] - dy[j])));
+        }
+    }
+    // delta = r / m_full; D+ = D + delta and u+ = u + D+, both Kahan-compensated
+    float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
+    XY<RPT, PAIR>::load_half(dc + bn, R, dcx, dcy);
+    XY<RPT, PAIR>::load_half(uc + bn, R, ucx, ucy);
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        float yx = ax[j] * nc.x - dcx[j], yy = ay[j] * nc.y - dcy[j];
+        float tx = dx[j] + yx, ty = dy[j] + yy;
+        dcx[j] = (tx - dx[j]) - yx;
+        dcy[j] = (ty - dy[j]) - yy;
+        dx[j] = tx;
+        dy[j] = ty;
+        float vx = tx - ucx[j], vy = ty - ucy[j];
+        float sx = unx[j] + vx, sy = uny[j] + vy;
+        ucx[j] = (sx - unx[j]) - vx;
+        ucy[j] = (sy - uny[j]) - vy;
+        ox[j] = sx;
+        oy[j] = sy;
+    }
+    XY<RPT, PAIR>::store(dh + bn, R, dx, dy);
+    XY<RPT, PAIR>::store_half(dc + bn, R, dcx, dcy);
+    XY<RPT, PAIR>::store_half(uc + bn, R, ucx, ucy);
+    XY<RPT, PAIR>::store(uhn + bn, R, ox, oy);
+}
+
 // The fused step for one non-hanging node and RPT right-hand sides.  The
 // corners of each term's element come from the per-term copy m.tcorn, loaded
 // beside the term itself (not from econn after it), so the gather chain is
@@ -443,56 +505,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
             q4_corner_acc<float>(f, vx, vy, ax[j], ay[j]);
         }
     }
-    // dashpot term -2 a2 C D (zero away from the absorbing boundary)
-    const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
-    float dx[RPT], dy[RPT];
-    XY<RPT, PAIR>::load_cg(dh + bn, R, dx, dy);
-    if (nc.z != 0.f || nc.w != 0.f) {
-#pragma unroll
-        for (int j = 0; j < RPT; ++j) { ax[j] += nc.z * dx[j]; ay[j] += nc.w * dy[j]; }
-    }
-    float unx[RPT], uny[RPT];
-    XY<RPT, PAIR>::load(uh + bn, R, unx, uny);
-    // hanging nodes this node anchors:
-    //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_h - u_n) + (D_h - D_n)) ]
-    // (u_h, D_h from the hanging node's rows, which change only in k_hang32;
-    // the other anchor's row is rewritten in place during this kernel)
-    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
-        int h = __ldg(m.llist + 2 * q);
-        float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
-        I bh = ((I)h * 2) * R + roff;
-        float hx[RPT], hy[RPT], uhx[RPT], uhy[RPT];
-        XY<RPT, PAIR>::load_cg(dh + bh, R, hx, hy);
-        XY<RPT, PAIR>::load(uh + bh, R, uhx, uhy);
-#pragma unroll
-        for (int j = 0; j < RPT; ++j) {
-            ax[j] += 0.5f * (hc.x * hx[j] + hc.z * ((uhx[j] - unx[j]) + (hx[j] - dx[j])));
-            ay[j] += 0.5f * (hc.y * hy[j] + hc.w * ((uhy[j] - uny[j]) + (hy[j] - dy[j])));
-        }
-    }
-    // delta = r / m_full; D+ = D + delta and u+ = u + D+, both Kahan-compensated
-    float dcx[RPT], dcy[RPT], ucx[RPT], ucy[RPT], ox[RPT], oy[RPT];
-    XY<RPT, PAIR>::load_half(dc + bn, R, dcx, dcy);
-    XY<RPT, PAIR>::load_half(uc + bn, R, ucx, ucy);
-#pragma unroll
-    for (int j = 0; j < RPT; ++j) {
-        float yx = ax[j] * nc.x - dcx[j], yy = ay[j] * nc.y - dcy[j];
-        float tx = dx[j] + yx, ty = dy[j] + yy;
-        dcx[j] = (tx - dx[j]) - yx;
-        dcy[j] = (ty - dy[j]) - yy;
-        dx[j] = tx;
-        dy[j] = ty;
-        float vx = tx - ucx[j], vy = ty - ucy[j];
-        float sx = unx[j] + vx, sy = uny[j] + vy;
-        ucx[j] = (sx - unx[j]) - vx;
-        ucy[j] = (sy - uny[j]) - vy;
-        ox[j] = sx;
-        oy[j] = sy;
-    }
-    XY<RPT, PAIR>::store(dh + bn, R, dx, dy);
-    XY<RPT, PAIR>::store_half(dc + bn, R, dcx, dcy);
-    XY<RPT, PAIR>::store_half(uc + bn, R, ucx, ucy);
-    XY<RPT, PAIR>::store(uhn + bn, R, ox, oy);
+    node_update<RPT, PAIR, I>(m, n, bn, R, roff, ax, ay, uh, uhn, uc, dh, dc);
 }
 
 // Tiled variant of k_step32: a block owns `tn` consecutive active nodes (a
@@ -963,6 +976,186 @@ __global__ void __launch_bounds__(544) k_pipe32(DevModel m, PipeArgs pa, const f
     }
 }
 
+// ---- tensor-core step (variant 3) ------------------------------------------
+// The element products K_e u_e of the batched form on the 5th-generation
+// tensor cores (tcgen05, kind::tf32).  A block owns a tile of at most kMmaTn
+// consecutive active nodes (closed early where their terms would read more
+// than kMmaEmax distinct elements) and kMmaRc right-hand sides.  With
+// K_e = mu_e Kmu + lambda_e Klambda (calck is linear in (mu, lambda),
+// formulation.f90:276-313), every distinct element of the tile's terms
+// (at most kMmaEmax) contributes one row per right-hand side: its 8 corner
+// dofs u_e relative to corner 0 (K has the rigid translations in its null
+// space, so K (u_e - u_0) = K u_e, and the differences are small).  The rows
+// meet B = [Kmu; Klambda] (16 x 8) in 128 x 16 x 8 MMAs, 8 elements x 16
+// right-hand sides each, in 3xTF32: A_hi B_hi + A_hi B_lo + A_lo B_hi, with
+// hi = tf32(x) and lo = tf32(x - hi), which holds FP32-level accuracy.  One
+// thread issues every MMA of the tile and commits them to an mbarrier; the
+// four warps read D = (Kmu u_e, Klambda u_e) back from TMEM, scale by
+// (mu_e, lambda_e) into per-element corner forces in shared memory (over the
+// A tiles, which the MMAs no longer read), and then each thread finishes a
+// node for four right-hand sides: its DRM terms, its element terms (the
+// forces of its corner, at weight 1 or 1/2), and node_update.  The plain
+// state layout (value of node n, dof d, rhs r at (n*2 + d)*R + r).
+struct MmaArgs {
+    const int *nptr;              // per tile: first active node
+    const int *eptr, *elist;      // per tile: its distinct elements
+    const unsigned char *tj;      // per gather term: its element's index in the tile
+    const float *btile;           // [Kmu; Klambda] split into tf32 hi then lo, 128 floats each, K-major layout
+    long long wait_cycles;        // bound of the MMA completion wait
+};
+
+constexpr int kMmaRc = 16;        // right-hand sides per block
+constexpr int kMmaTn = 32;        // nodes per tile
+constexpr int kMmaEmax = 64;      // elements per tile (8 MMA row chunks of 8 elements x 16 RHS)
+constexpr int kMmaThreads = 256;  // kMmaTn nodes x kMmaRc / 2 right-hand sides per thread
+constexpr unsigned kMmaTmemCols = 128;   // 8 chunks x 16 FP32 columns
+constexpr unsigned kMmaAbytes = kMmaEmax * kMmaRc * 32;   // one A tile (hi or lo)
+constexpr unsigned kMmaSmem = 1024 + 2 * kMmaAbytes;       // B hi/lo, A hi, A lo
+
+__global__ void __launch_bounds__(kMmaThreads) k_mma32(DevModel m, MmaArgs ma, const float *__restrict__ uh,
+                                                       float *__restrict__ uhn, unsigned short *__restrict__ uc,
+                                                       float *__restrict__ dh, unsigned short *__restrict__ dc) {
+    extern __shared__ __align__(128) unsigned char smtc[];   // 16-byte alignment suffices without swizzle
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ uint32_t tslot;
+    unsigned char *sAhi = smtc + 1024, *sAlo = sAhi + kMmaAbytes;
+    float *sF = reinterpret_cast<float *>(sAhi);   // after the MMAs: force (j*8 + k)*kMmaRc + r
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tile = blockIdx.x, rbase = blockIdx.y * kMmaRc;
+    const size_t R = (size_t)m.R;
+    const int e0 = __ldg(ma.eptr + tile), ne_t = __ldg(ma.eptr + tile + 1) - e0;
+    const int nchunk = (ne_t + 7) >> 3;
+    for (int i = tid; i < 64; i += kMmaThreads)
+        reinterpret_cast<float4 *>(smtc)[i] = __ldg(reinterpret_cast<const float4 *>(ma.btile) + i);
+    // every load of the thread's rows first (at most four rows a thread), then
+    // the differences, splits and stores
+    constexpr int kRowsPerThread = kMmaEmax * kMmaRc / kMmaThreads;
+    float ux[kRowsPerThread][4], uy[kRowsPerThread][4];
+#pragma unroll
+    for (int i = 0; i < kRowsPerThread; ++i) {
+        const int row = tid + i * kMmaThreads, j = row >> 4, r = row & 15;
+        if (row < nchunk * 128 && j < ne_t) {
+            const int4 cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + __ldg(ma.elist + e0 + j));
+            const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const size_t b = (size_t)cc[q] * 2 * R + rbase + r;
+                ux[i][q] = __ldg(uh + b);
+                uy[i][q] = __ldg(uh + b + R);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) { ux[i][q] = 0.f; uy[i][q] = 0.f; }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kRowsPerThread; ++i) {
+        const int row = tid + i * kMmaThreads;
+        if (row >= nchunk * 128) continue;
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            v[2 * q] = ux[i][q] - ux[i][0];
+            v[2 * q + 1] = uy[i][q] - uy[i][0];
+        }
+        float hi[8], lo[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            hi[k] = tc_tf32(v[k]);
+            lo[k] = tc_tf32(v[k] - hi[k]);
+        }
+        const unsigned o = tc_kmaj_off(row, 0);
+        *reinterpret_cast<float4 *>(sAhi + o) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<float4 *>(sAhi + o + kTcLbo) = make_float4(hi[4], hi[5], hi[6], hi[7]);
+        *reinterpret_cast<float4 *>(sAlo + o) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        *reinterpret_cast<float4 *>(sAlo + o + kTcLbo) = make_float4(lo[4], lo[5], lo[6], lo[7]);
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc_alloc(smem_addr(&tslot), kMmaTmemCols);
+    // the A and B tiles (generic-proxy stores) become visible to the MMAs
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = tslot;
+    if (tid == 0) {
+        const uint32_t idesc = tc_idesc_tf32(128, 16);
+        const unsigned sb = smem_addr(smtc);
+        const uint64_t bh = tc_smem_desc(sb), bl = tc_smem_desc(sb + 512);
+        for (int c = 0; c < nchunk; ++c) {
+            const uint64_t ah = tc_smem_desc(smem_addr(sAhi) + 4096u * c);
+            const uint64_t al = tc_smem_desc(smem_addr(sAlo) + 4096u * c);
+            const uint32_t d = tbase + 16u * c;
+            tc_mma_tf32(d, ah, bh, idesc, 0);
+            tc_mma_tf32(d, ah, bl, idesc, 1);
+            tc_mma_tf32(d, al, bh, idesc, 1);
+        }
+        tc_commit(smem_addr(&mbar));
+    }
+    bool ok = mbar_wait_bounded(smem_addr(&mbar), 0u, ma.wait_cycles);
+    if (!ok) {
+        if (lane == 0) atomicOr(m.d_flag, 2);
+        // the MMAs must have finished before their TMEM is freed
+        ok = mbar_wait_bounded(smem_addr(&mbar), 0u, PIPE_WAIT_CYCLES);
+    }
+    tc_fence_after();
+    const bool all_ok = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (all_ok) {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 of every other chunk
+        const int quarter = warp & 3;
+        for (int c = warp >> 2; c < nchunk; c += kMmaThreads / 128) {
+            float d[16];
+            tc_ld16(tbase + ((uint32_t)(32 * quarter) << 16) + 16u * c, d);
+            const int row = c * 128 + 32 * quarter + lane, j = row >> 4, r = row & 15;
+            if (j < ne_t) {
+                const float4 k4 = __ldg(reinterpret_cast<const float4 *>(m.ecoef32) + __ldg(ma.elist + e0 + j));
+                const float mu = 4.f * k4.z, lam = 4.f * k4.y;   // ecoef32 = ((l+2m)/4, l/4, m/4, (l+3m)/12)
+#pragma unroll
+                for (int k = 0; k < 8; ++k) sF[(j * 8 + k) * kMmaRc + r] = mu * d[k] + lam * d[8 + k];
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tbase, kMmaTmemCols);
+    if (!all_ok) return;
+    constexpr int RPT = kMmaRc * kMmaTn / kMmaThreads;   // right-hand sides per thread
+    constexpr int TPN = kMmaRc / RPT;                     // threads per node
+    const int n = __ldg(ma.nptr + tile) + tid / TPN;
+    if (n >= __ldg(ma.nptr + tile + 1)) return;
+    const int r0 = (tid % TPN) * RPT;
+    const size_t roff = (size_t)rbase + r0;
+    const size_t bn = ((size_t)n * 2) * R + roff;
+    float ax[RPT], ay[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) { ax[j] = 0.f; ay[j] = 0.f; }
+    for (int q = m.dptr[n]; q < m.dptr[n + 1]; ++q) {
+        int ent = __ldg(m.dlist + q);
+        float w = (ent & 1) ? 0.5f : 1.0f;
+        int sc = ent >> 1;
+        size_t b = ((size_t)(sc >> 2) * 8 + 2 * (sc & 3)) * R + roff;
+        float fx[RPT], fy[RPT];
+        XY<RPT, false>::load_cg(m.fdrm32 + b, R, fx, fy);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
+    }
+    for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
+        const int ent = __ldg(m.tlist + q);
+        const float w = (ent & 1) ? 0.5f : 1.0f;
+        const int c = (ent >> 1) & 3, j = __ldg(ma.tj + q);
+        const float *fx = sF + (j * 8 + 2 * c) * kMmaRc + r0, *fy = fx + kMmaRc;
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            ax[k] -= w * fx[k];
+            ay[k] -= w * fy[k];
+        }
+    }
+    node_update<RPT, false, size_t>(m, n, bn, R, roff, ax, ay, uh, uhn, uc, dh, dc);
+}
+
 // Point source in the FP32 form, after the step kernel and before k_hang32
 // (the force enters delta linearly, so the step kernels stay untouched).
 //   POINTN: the y dof of node p32_node[i] gets w_i f(t) / m_full added to D+
@@ -1272,6 +1465,60 @@ static int pipe_setup(Ctx &c) {
     return EXFEM_OK;
 }
 
+// [Kmu; Klambda] of the square Q4 element (the stiffness for (mu, lambda) =
+// (1, 0) and (0, 1), from the closed form of q4_fold/q4_corner_acc in FP64:
+// row 2c + d is the force on corner c, dof d, for unit corner dofs), split
+// into tf32 hi and lo parts and laid out as the K-major operand tile.
+static std::vector<float> mma_btile() {
+    auto tf32 = [](double x) {   // round to nearest, ties away, to a 10-bit mantissa
+        float f = (float)x;
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        u = (u + 0x1000u) & 0xFFFFE000u;
+        std::memcpy(&f, &u, 4);
+        return f;
+    };
+    std::vector<float> out(256, 0.f);
+    for (int part = 0; part < 2; ++part) {     // mu, lambda
+        const double mu = part == 0 ? 1.0 : 0.0, lam = part == 0 ? 0.0 : 1.0;
+        const double A = (lam + 2 * mu) / 4, B = lam / 4, Cc = mu / 4, D = (lam + 3 * mu) / 12;
+        for (int c = 0; c < 4; ++c)
+            for (int j = 0; j < 8; ++j) {
+                double ux[4] = {0, 0, 0, 0}, uy[4] = {0, 0, 0, 0};
+                (j & 1 ? uy : ux)[j >> 1] = 1.0;
+                double ax = 0.0, ay = 0.0;
+                q4_corner_acc<double>(q4_fold<double>(A, B, Cc, D, c, 1.0), ux, uy, ax, ay);
+                for (int d = 0; d < 2; ++d) {
+                    const double kv = -(d == 0 ? ax : ay);   // K[2c + d][j]
+                    const int n = part * 8 + 2 * c + d;
+                    const float hi = tf32(kv), lo = tf32(kv - (double)hi);
+                    const int off = ((n >> 3) * (int)kTcSbo + (j >> 2) * (int)kTcLbo + (n & 7) * 16 + (j & 3) * 4) / 4;
+                    out[off] = hi;
+                    out[128 + off] = lo;
+                }
+            }
+    }
+    return out;
+}
+
+static int mma_setup(Ctx &c) {
+    const Plan &P = c.plan;
+    MmaTiles T;
+    std::string why;
+    if (!build_mma_tiles(P, kMmaTn, kMmaEmax, T, why)) return EXFEM_OK;   // the direct gather runs
+    int rc;
+    if ((rc = upload32(c, T.nptr, &c.mma_nptr)) || (rc = upload32(c, T.eptr, &c.mma_eptr)) ||
+        (rc = upload32(c, T.elist, &c.mma_elist)) ||
+        (rc = upload32(c, T.tj, &c.mma_tj)) || (rc = upload32(c, mma_btile(), &c.mma_btile)))
+        return rc;
+    CK(cudaFuncSetAttribute(k_mma32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMmaSmem));
+    c.mma_ntiles = T.ntiles;
+    c.rhs_per_thread = kMmaRc * kMmaTn / kMmaThreads;
+    c.block_threads = kMmaThreads;
+    c.use_mma = true;
+    return EXFEM_OK;
+}
+
 int f32_alloc(Ctx &c) {
     const Plan &P = c.plan;
     DevModel &m = c.dm;
@@ -1379,9 +1626,15 @@ int f32_alloc(Ctx &c) {
     if (c.opts.variant == 2 && P.R % 4 == 0) {
         if ((rc = pipe_setup(c))) return rc;
     }
+    // tensor-core step (variant 3): R a multiple of kMmaRc and every tile
+    // within kMmaEmax elements; otherwise the direct gather runs
+    c.use_mma = false;
+    if (c.opts.variant == 3 && P.R % kMmaRc == 0) {
+        if ((rc = mma_setup(c))) return rc;
+    }
     // the direct gather with several threads per node groups the state by
     // the thread's RHS (the tiled variants read the plain layout)
-    const bool direct = !c.use_tiles && !c.use_pipe;
+    const bool direct = !c.use_tiles && !c.use_pipe && !c.use_mma;
     m.lg = (direct && c.rhs_per_thread < P.R && f32_interleave(P.R)) ? c.rhs_per_thread : P.R;
     // the direct gather's per-term corner copies (with few RHS k_step32
     // reads the corners from econn)
@@ -1422,7 +1675,8 @@ static void f32_set_shape(Ctx &c, int rpt, int block) {
 // reset), at most min(nsteps, 4) of them, so the receiver slots they write
 // stay inside the seismogram buffer; init_explicit then clears it all.
 int f32_tune_in_place(Ctx &c) {
-    if (c.use_tiles || c.use_pipe || c.opts.rhs_per_thread > 0 || c.opts.block_threads > 0) return EXFEM_OK;
+    if (c.use_tiles || c.use_pipe || c.use_mma || c.opts.rhs_per_thread > 0 || c.opts.block_threads > 0)
+        return EXFEM_OK;
     const int nst = std::min(c.plan.nsteps, 4);
     if (nst < 2) return EXFEM_OK;
     cudaEvent_t a = nullptr, b = nullptr;
@@ -1495,7 +1749,14 @@ int f32_launch_step(Ctx &c, int par) {
     const int T = c.block_threads;
     const int rpt = c.rhs_per_thread;
     long long work = (long long)m.n_active * (m.R / rpt);
-    if (c.use_pipe) {
+    if (c.use_mma) {
+        MmaArgs ma{c.mma_nptr, c.mma_eptr, c.mma_elist, c.mma_tj, c.mma_btile,
+                   c.opts.wait_cycles > 0 ? (long long)c.opts.wait_cycles : PIPE_WAIT_CYCLES};
+        k_mma32<<<dim3(c.mma_ntiles, m.R / kMmaRc), kMmaThreads, kMmaSmem, c.stream>>>(m, ma, uh, uhn, c.ucomp,
+                                                                                      c.udel[0], c.dcomp);
+        c.launches++;
+        mark(c, "k_mma32");
+    } else if (c.use_pipe) {
         PipeArgs pa{static_cast<const int4 *>(c.p_hdr), static_cast<const int2 *>(c.p_runs),
                     static_cast<const int4 *>(c.p_nrec), static_cast<const int4 *>(c.p_tpack), c.t_lslot,
                     c.tile_tn, c.tile_n, c.pipe_nstage, c.pipe_stage,

@@ -811,35 +811,45 @@ int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err) {
 
 bool build_mma_tiles(const Plan &P, int tn, int emax_limit, MmaTiles &T, std::string &why) {
     T = MmaTiles();
-    if (tn < 1 || emax_limit < 1 || emax_limit > 255) { why = "bad tile shape"; return false; }
+    if (tn < 1 || emax_limit < 8 || emax_limit > 255) { why = "bad tile shape"; return false; }
     T.tn = tn;
-    T.ntiles = (P.n_active + tn - 1) / tn;
-    T.eptr.assign(T.ntiles + 1, 0);
     T.tj.assign(P.tlist.size(), 0);
-    std::vector<int> local(P.ne, -1), elems;
-    for (int t = 0; t < T.ntiles; ++t) {
-        const int n0 = t * tn, n1 = std::min(P.n_active, n0 + tn);
+    T.nptr.push_back(0);
+    T.eptr.push_back(0);
+    std::vector<int> local(P.ne, -1), elems, fresh;
+    int n = 0;
+    while (n < P.n_active) {
+        const int n0 = n;
         elems.clear();
-        for (int n = n0; n < n1; ++n)
+        while (n < P.n_active && n - n0 < tn) {
+            // the node's new elements; it joins the tile only if they fit
+            fresh.clear();
             for (int q = P.tptr[n]; q < P.tptr[n + 1]; ++q) {
                 const int e = (P.tlist[q] >> 1) >> 2;
-                if (local[e] < 0) {
-                    local[e] = (int)elems.size();
-                    elems.push_back(e);
-                }
-                T.tj[q] = (unsigned char)std::min(local[e], 255);
+                if (local[e] < 0 && std::find(fresh.begin(), fresh.end(), e) == fresh.end()) fresh.push_back(e);
             }
-        if ((int)elems.size() > emax_limit) {
-            why = "tile " + std::to_string(t) + " reads " + std::to_string(elems.size()) + " elements (limit " +
-                  std::to_string(emax_limit) + ")";
-            for (int e : elems) local[e] = -1;
-            return false;
+            if ((int)(elems.size() + fresh.size()) > emax_limit) {
+                if (n == n0) {
+                    why = "node " + std::to_string(n) + " reads more than " + std::to_string(emax_limit) + " elements";
+                    for (int e : elems) local[e] = -1;
+                    return false;
+                }
+                break;
+            }
+            for (int e : fresh) {
+                local[e] = (int)elems.size();
+                elems.push_back(e);
+            }
+            for (int q = P.tptr[n]; q < P.tptr[n + 1]; ++q) T.tj[q] = (unsigned char)local[(P.tlist[q] >> 1) >> 2];
+            ++n;
         }
         T.emax = std::max(T.emax, (int)elems.size());
         T.elist.insert(T.elist.end(), elems.begin(), elems.end());
-        T.eptr[t + 1] = (int)T.elist.size();
+        T.eptr.push_back((int)T.elist.size());
+        T.nptr.push_back(n);
         for (int e : elems) local[e] = -1;
     }
+    T.ntiles = (int)T.nptr.size() - 1;
     return true;
 }
 

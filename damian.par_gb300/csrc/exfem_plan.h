@@ -151,18 +151,21 @@ struct Tiles {
 
 int build_tiles(const Plan &P, int tn, Tiles &T, std::string &err);
 
-// Element tiles of the tensor-core FP32 step (variant 3): tiles of tn
-// consecutive active nodes, each with the distinct elements its terms read
-// (their K.u is computed once per tile), and per term the element's index in
-// its tile's list.
+// Element tiles of the tensor-core FP32 step (variant 3): runs of at most tn
+// consecutive active nodes whose terms read at most emax_limit distinct
+// elements (a tile closes early where the Morton order jumps between
+// regions), each with its distinct elements (their K.u is computed once per
+// tile), and per term the element's index in its tile's list.
 struct MmaTiles {
     int tn = 0, ntiles = 0;
     int emax = 0;                      // most elements in a tile
+    std::vector<int> nptr;             // per tile: first active node (ntiles + 1)
     std::vector<int> eptr, elist;      // per tile: its elements (internal ids)
     std::vector<unsigned char> tj;     // per gather term: index of its element in the tile's list
 };
 
-// Fails (false, with why) when a tile has more than emax_limit elements.
+// Fails (false, with why) only when one node alone reads more than
+// emax_limit elements.
 bool build_mma_tiles(const Plan &P, int tn, int emax_limit, MmaTiles &T, std::string &why);
 
 // Per active node, the FP32 step's node coefficients: 1/m_full (x, y) and

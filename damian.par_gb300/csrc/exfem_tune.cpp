@@ -2,8 +2,9 @@
 //
 // It times every candidate shape of the FP32 form on the caller's own model
 // and keeps the fastest: kernel variant (0 direct gather, 1 shared-memory
-// tiles, 2 bulk-copy pipeline when nrhs is a multiple of 4), block size
-// (128, 256, 512) and right-hand sides per thread (1, 2, 4 dividing nrhs).
+// tiles, 2 bulk-copy pipeline when nrhs is a multiple of 4, 3 tensor-core
+// step when nrhs is a multiple of 16), block size (128, 256, 512) and
+// right-hand sides per thread (1, 2, 4 dividing nrhs).
 // Each candidate gets its own context (exfem_gpu_create with that shape), a
 // few warm-up steps, and a burst timed with CUDA events on the context's
 // stream (exfem_gpu_run_timed).  Results are cached in the process per
@@ -84,11 +85,13 @@ int autotune_shapes(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opt
     std::vector<int> variants = {0};
     if (max_variant >= 1) variants.push_back(1);
     if (max_variant >= 2 && R % 4 == 0) variants.push_back(2);
+    if (max_variant >= 3 && R % 16 == 0) variants.push_back(3);
     TuneVal best{-1, 0, 0, 0.0};
     for (int v : variants)
         for (int rpt : {1, 2, 4}) {
-            if (R % rpt) continue;
+            if (R % rpt || (v == 3 && rpt != 2)) continue;   // the tensor-core step has one shape
             for (int bt : {128, 256, 512}) {
+                if (v == 3 && bt != 256) continue;
                 exfem_opts o = *opts;
                 o.variant = v;
                 o.block_threads = bt;
@@ -113,5 +116,5 @@ int autotune_shapes(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opt
 
 extern "C" int exfem_gpu_autotune(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opts *opts, int steps,
                                   double *ms_per_step) {
-    return exfem::autotune_shapes(mesh, prob, opts, steps, 2, ms_per_step);
+    return exfem::autotune_shapes(mesh, prob, opts, steps, 3, ms_per_step);
 }

@@ -134,7 +134,11 @@ typedef struct exfem_opts {
                           (default), 1 = shared-memory tiled step, 2 = tiles
                           streamed by bulk copies through a two-stage
                           shared-memory pipeline (persistent grid; needs nrhs
-                          a multiple of 4, else the direct gather runs)       */
+                          a multiple of 4, else the direct gather runs),
+                          3 = element products on the tensor cores (tcgen05
+                          kind::tf32 in 3xTF32; needs nrhs a multiple of 16
+                          and at most 64 elements per 32-node tile, else the
+                          direct gather runs)                               */
     int index_bits;    /* FP32 direct gather: 0 = 32-bit indices when every
                           thread id and array index fits, else 64; 64 = always
                           64-bit (same results)                               */
@@ -272,7 +276,8 @@ int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const do
 /* Autotuner of the FP32 form (opts->precision must be EXFEM_FP32_KAHAN).
  * Times every candidate shape on this mesh and problem and writes the
  * fastest into opts: variant (0 direct gather, 1 shared-memory tiles, 2
- * bulk-copy pipeline when the right-hand sides are a multiple of 4),
+ * bulk-copy pipeline when the right-hand sides are a multiple of 4, 3
+ * tensor-core step when they are a multiple of 16),
  * block_threads (128, 256, 512) and rhs_per_thread (1, 2, 4).  Each
  * candidate runs in a context of its own (one at a time: the device must
  * hold one more context of this problem), 3 warm-up steps and `steps` steps

@@ -47,7 +47,8 @@ def test_canyon_fp32_every_rhs_vs_oracle(variant):
         assert per_receiver_rel(g[r], o["seis"]).max() <= TOL, r
 
 
-@pytest.mark.parametrize("variant,rpt", [(0, 1), (0, 2), (0, 4), (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4)])
+@pytest.mark.parametrize("variant,rpt", [(0, 1), (0, 2), (0, 4), (1, 1), (1, 2), (1, 4), (2, 1), (2, 2), (2, 4),
+                                         (3, 4)])
 def test_batched_valley_rhs_match_oracle_for_every_kernel_and_tile(variant, rpt):
     m = workloads.build("valley_batched", scale=0.1, steps=500, save_every=5)
     assert m.problem.nrhs == 64
@@ -382,3 +383,34 @@ def test_in_context_tuning_keeps_results(nrhs_waves):
     assert np.array_equal(a, b)
     for r in range(m.problem.nrhs):
         assert np.array_equal(ua[r], ub[r]), r
+
+
+def test_tensor_core_step_runs_and_matches_the_direct_gather():
+    """Variant 3: the element products on the tensor cores (k_mma32, tcgen05
+    kind::tf32 in 3xTF32) are what runs; on the 64-RHS valley and on a
+    16-RHS refined canyon (hanging nodes, DRM layer) every RHS stays within
+    the FP32 tolerance of the direct gather, and the canyon's RHS match the
+    oracle.  With 8 RHS (not a multiple of 16) the direct gather runs."""
+    mv = workloads.build("valley_batched", scale=0.1, steps=40, save_every=2)
+    with Solver(mv, precision=EXFEM_FP32_KAHAN, variant=3) as s:
+        s.init_explicit()
+        names = s.kernel_times(4)
+    assert "k_mma32" in names and "k_step32" not in names, names
+    a, _ = run32(mv, variant=0)
+    b, _ = run32(mv, variant=3)
+    for r in range(mv.problem.nrhs):
+        assert per_receiver_rel(b[r], a[r]).max() <= TOL, r
+    mc = workloads.build("canyon", scale=0.2, steps=300, save_every=3, waves=EIGHT_WAVES + EIGHT_WAVES)
+    assert mc.problem.nrhs == 16 and mc.problem.nhanging > 0
+    a, _ = run32(mc, variant=0)
+    b, _ = run32(mc, variant=3)
+    for r in range(16):
+        assert per_receiver_rel(b[r], a[r]).max() <= TOL, r
+    for r in (0, 13):
+        o = oracle.run(mc, rhs=r, nthreads=NT)
+        assert per_receiver_rel(b[r], o["seis"]).max() <= TOL, r
+    m8 = workloads.build("canyon", scale=0.15, steps=20, waves=EIGHT_WAVES)
+    with Solver(m8, precision=EXFEM_FP32_KAHAN, variant=3) as s:
+        s.init_explicit()
+        names = s.kernel_times(2)
+    assert "k_step32" in names and "k_mma32" not in names, names
