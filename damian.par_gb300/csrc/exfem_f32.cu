@@ -1021,7 +1021,10 @@ __global__ void __launch_bounds__(kMmaThreads) k_mma32(DevModel m, MmaArgs ma, c
     unsigned char *sAhi = smtc + 1024, *sAlo = sAhi + kMmaAbytes;
     float *sF = reinterpret_cast<float *>(sAhi);   // after the MMAs: force (j*8 + k)*kMmaRc + r
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tile = blockIdx.x, rbase = blockIdx.y * kMmaRc;
+    // the RHS chunks of a tile are adjacent blocks, so they meet the tile's
+    // metadata and the same state rows in L2 together
+    const int nch = m.R / kMmaRc;
+    const int tile = (int)(blockIdx.x / nch), rbase = (int)(blockIdx.x % nch) * kMmaRc;
     const size_t R = (size_t)m.R;
     const int e0 = __ldg(ma.eptr + tile), ne_t = __ldg(ma.eptr + tile + 1) - e0;
     const int nchunk = (ne_t + 7) >> 3;
@@ -1465,42 +1468,6 @@ static int pipe_setup(Ctx &c) {
     return EXFEM_OK;
 }
 
-// [Kmu; Klambda] of the square Q4 element (the stiffness for (mu, lambda) =
-// (1, 0) and (0, 1), from the closed form of q4_fold/q4_corner_acc in FP64:
-// row 2c + d is the force on corner c, dof d, for unit corner dofs), split
-// into tf32 hi and lo parts and laid out as the K-major operand tile.
-static std::vector<float> mma_btile() {
-    auto tf32 = [](double x) {   // round to nearest, ties away, to a 10-bit mantissa
-        float f = (float)x;
-        uint32_t u;
-        std::memcpy(&u, &f, 4);
-        u = (u + 0x1000u) & 0xFFFFE000u;
-        std::memcpy(&f, &u, 4);
-        return f;
-    };
-    std::vector<float> out(256, 0.f);
-    for (int part = 0; part < 2; ++part) {     // mu, lambda
-        const double mu = part == 0 ? 1.0 : 0.0, lam = part == 0 ? 0.0 : 1.0;
-        const double A = (lam + 2 * mu) / 4, B = lam / 4, Cc = mu / 4, D = (lam + 3 * mu) / 12;
-        for (int c = 0; c < 4; ++c)
-            for (int j = 0; j < 8; ++j) {
-                double ux[4] = {0, 0, 0, 0}, uy[4] = {0, 0, 0, 0};
-                (j & 1 ? uy : ux)[j >> 1] = 1.0;
-                double ax = 0.0, ay = 0.0;
-                q4_corner_acc<double>(q4_fold<double>(A, B, Cc, D, c, 1.0), ux, uy, ax, ay);
-                for (int d = 0; d < 2; ++d) {
-                    const double kv = -(d == 0 ? ax : ay);   // K[2c + d][j]
-                    const int n = part * 8 + 2 * c + d;
-                    const float hi = tf32(kv), lo = tf32(kv - (double)hi);
-                    const int off = ((n >> 3) * (int)kTcSbo + (j >> 2) * (int)kTcLbo + (n & 7) * 16 + (j & 3) * 4) / 4;
-                    out[off] = hi;
-                    out[128 + off] = lo;
-                }
-            }
-    }
-    return out;
-}
-
 static int mma_setup(Ctx &c) {
     const Plan &P = c.plan;
     MmaTiles T;
@@ -1509,9 +1476,10 @@ static int mma_setup(Ctx &c) {
     int rc;
     if ((rc = upload32(c, T.nptr, &c.mma_nptr)) || (rc = upload32(c, T.eptr, &c.mma_eptr)) ||
         (rc = upload32(c, T.elist, &c.mma_elist)) ||
-        (rc = upload32(c, T.tj, &c.mma_tj)) || (rc = upload32(c, mma_btile(), &c.mma_btile)))
+        (rc = upload32(c, T.tj, &c.mma_tj)) || (rc = upload32(c, tc_b_operand_q4(), &c.mma_btile)))
         return rc;
     CK(cudaFuncSetAttribute(k_mma32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMmaSmem));
+    if ((long long)T.ntiles * (P.R / kMmaRc) >= (1LL << 31)) return EXFEM_OK;   // grid limit: the direct gather runs
     c.mma_ntiles = T.ntiles;
     c.rhs_per_thread = kMmaRc * kMmaTn / kMmaThreads;
     c.block_threads = kMmaThreads;
@@ -1752,8 +1720,8 @@ int f32_launch_step(Ctx &c, int par) {
     if (c.use_mma) {
         MmaArgs ma{c.mma_nptr, c.mma_eptr, c.mma_elist, c.mma_tj, c.mma_btile,
                    c.opts.wait_cycles > 0 ? (long long)c.opts.wait_cycles : PIPE_WAIT_CYCLES};
-        k_mma32<<<dim3(c.mma_ntiles, m.R / kMmaRc), kMmaThreads, kMmaSmem, c.stream>>>(m, ma, uh, uhn, c.ucomp,
-                                                                                      c.udel[0], c.dcomp);
+        k_mma32<<<(unsigned)c.mma_ntiles * (unsigned)(m.R / kMmaRc), kMmaThreads, kMmaSmem, c.stream>>>(
+            m, ma, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
         c.launches++;
         mark(c, "k_mma32");
     } else if (c.use_pipe) {

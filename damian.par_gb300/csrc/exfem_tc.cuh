@@ -12,6 +12,10 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "exfem_device.cuh"
 
 namespace exfem {
 
@@ -88,6 +92,42 @@ __device__ __forceinline__ float tc_tf32(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return __uint_as_float(r);
+}
+
+// [Kmu; Klambda] of the square Q4 element (the stiffness for (mu, lambda) =
+// (1, 0) and (0, 1), from the closed form of q4_fold/q4_corner_acc in FP64:
+// row 2c + d is the force on corner c, dof d, for unit corner dofs), split
+// into tf32 hi and lo parts and laid out as the K-major operand tile.
+inline std::vector<float> tc_b_operand_q4() {
+    auto tf32 = [](double x) {   // round to nearest, ties away, to a 10-bit mantissa
+        float f = (float)x;
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        u = (u + 0x1000u) & 0xFFFFE000u;
+        std::memcpy(&f, &u, 4);
+        return f;
+    };
+    std::vector<float> out(256, 0.f);
+    for (int part = 0; part < 2; ++part) {     // mu, lambda
+        const double mu = part == 0 ? 1.0 : 0.0, lam = part == 0 ? 0.0 : 1.0;
+        const double A = (lam + 2 * mu) / 4, B = lam / 4, Cc = mu / 4, D = (lam + 3 * mu) / 12;
+        for (int c = 0; c < 4; ++c)
+            for (int j = 0; j < 8; ++j) {
+                double ux[4] = {0, 0, 0, 0}, uy[4] = {0, 0, 0, 0};
+                (j & 1 ? uy : ux)[j >> 1] = 1.0;
+                double ax = 0.0, ay = 0.0;
+                q4_corner_acc<double>(q4_fold<double>(A, B, Cc, D, c, 1.0), ux, uy, ax, ay);
+                for (int d = 0; d < 2; ++d) {
+                    const double kv = -(d == 0 ? ax : ay);   // K[2c + d][j]
+                    const int n = part * 8 + 2 * c + d;
+                    const float hi = tf32(kv), lo = tf32(kv - (double)hi);
+                    const int off = ((n >> 3) * (int)kTcSbo + (j >> 2) * (int)kTcLbo + (n & 7) * 16 + (j & 3) * 4) / 4;
+                    out[off] = hi;
+                    out[128 + off] = lo;
+                }
+            }
+    }
+    return out;
 }
 
 }  // namespace exfem

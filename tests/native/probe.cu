@@ -8,6 +8,7 @@
 
 #include "exfem_device.cuh"
 #include "exfem_plan.h"
+#include "exfem_tc.cuh"
 
 using namespace exfem;
 
@@ -189,6 +190,29 @@ int probe_tiles(void *h, int tn, int *sizes, int *hptr, int *hlist, unsigned sho
     if (nslot) std::memcpy(nslot, T.nslot.data(), T.nslot.size() * sizeof(int));
     if (lslot && !T.lslot.empty()) std::memcpy(lslot, T.lslot.data(), T.lslot.size() * sizeof(int));
     return 0;
+}
+
+// Element tiles of the tensor-core step (build_mma_tiles): sizes[0..2] =
+// (ntiles, elements listed, most elements in a tile); nptr[ntiles + 1],
+// eptr[ntiles + 1], elist and tj[terms] are copied when non-NULL.  Returns 0,
+// or 1 when the builder refuses the model.
+int probe_mma_tiles(void *h, int tn, int emax, int *sizes, int *nptr, int *eptr, int *elist, unsigned char *tj) {
+    Plan &p = *static_cast<Plan *>(h);
+    MmaTiles T;
+    if (!build_mma_tiles(p, tn, emax, T, g_err)) return 1;
+    sizes[0] = T.ntiles; sizes[1] = (int)T.elist.size(); sizes[2] = T.emax;
+    if (nptr) std::memcpy(nptr, T.nptr.data(), T.nptr.size() * sizeof(int));
+    if (eptr) std::memcpy(eptr, T.eptr.data(), T.eptr.size() * sizeof(int));
+    if (elist && !T.elist.empty()) std::memcpy(elist, T.elist.data(), T.elist.size() * sizeof(int));
+    if (tj && !T.tj.empty()) std::memcpy(tj, T.tj.data(), T.tj.size());
+    return 0;
+}
+
+// The tensor-core step's B operand (tc_b_operand_q4): 256 floats, the tf32 hi
+// tile then the lo tile, in the K-major core-matrix layout.
+void probe_mma_btile(float *out) {
+    const std::vector<float> b = tc_b_operand_q4();
+    std::memcpy(out, b.data(), b.size() * sizeof(float));
 }
 
 // Halo runs of the tiles (the bulk copies of the pipelined step): fills

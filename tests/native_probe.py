@@ -15,7 +15,7 @@ sys.path.insert(0, PKG)
 from exfem.abi import ExfemError, Mesh, Problem  # noqa: E402
 
 SRC = [os.path.join(HERE, "native", "probe.cu"), os.path.join(PKG, "csrc", "exfem_plan.cpp")]
-DEPS = SRC + [os.path.join(PKG, "csrc", f) for f in ("exfem_plan.h", "exfem_device.cuh", "exfem_ctx.h")]
+DEPS = SRC + [os.path.join(PKG, "csrc", f) for f in ("exfem_plan.h", "exfem_device.cuh", "exfem_ctx.h", "exfem_tc.cuh")]
 OUT = os.path.join(HERE, "native", "_build", "libprobe.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 
@@ -68,6 +68,10 @@ def lib():
     L.probe_pipe_pack.restype = C.c_int
     L.probe_pipe_pack.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 4
     L.probe_tile_runs.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.probe_mma_tiles.restype = C.c_int
+    L.probe_mma_tiles.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 4
+    L.probe_mma_btile.restype = None
+    L.probe_mma_btile.argtypes = [C.c_void_p]
     L.probe_plan_wave.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, d]
     _lib = L
     return L
@@ -121,6 +125,21 @@ class PlanView:
         vp = lambda a: a.ctypes.data_as(C.c_void_p)
         assert L.probe_tiles(self.h, tn, sz, vp(hptr), vp(hlist), vp(tslot), vp(nslot), vp(lslot)) == 0
         return hptr, hlist[:nh], tslot.reshape(-1, 4), nslot, lslot[:len(self.llist) // 2], hmax
+
+    def mma_tiles(self, tn=32, emax=64):
+        """(nptr, eptr, elist, tj) of build_mma_tiles, or None when refused."""
+        L = lib()
+        sz = (C.c_int * 3)()
+        if L.probe_mma_tiles(self.h, tn, emax, sz, None, None, None, None) != 0:
+            return None
+        nt, nel = sz[0], sz[1]
+        nptr = np.zeros(nt + 1, np.int32)
+        eptr = np.zeros(nt + 1, np.int32)
+        elist = np.zeros(max(nel, 1), np.int32)
+        tj = np.zeros(max(len(self.tlist), 1), np.uint8)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        assert L.probe_mma_tiles(self.h, tn, emax, sz, vp(nptr), vp(eptr), vp(elist), vp(tj)) == 0
+        return nptr, eptr, elist[:nel], tj[:len(self.tlist)]
 
     def tile_runs(self, tn):
         """(rptr, runs (nruns, 2) as (first node, count)) of build_tiles."""

@@ -280,3 +280,47 @@ def test_fp32_increment_scheme_emulation_tracks_oracle():
     o = oracle.run(m, rhs=4, nthreads=8)
     e = emulate.emulate_fp32(m, 900, rhs=4)
     assert per_receiver_rel(e["seis"], o["seis"]).max() < 1e-5
+
+
+def test_tensor_core_tiles_cover_every_term():
+    """build_mma_tiles (the tensor-core step's tiles): consecutive runs of at
+    most 32 active nodes covering them all, at most 64 distinct elements per
+    tile, and every gather term's index naming its own element in its tile's
+    list."""
+    m = workloads.build("valley_batched", scale=0.1, steps=4)
+    P = npb.PlanView(m)
+    nptr, eptr, elist, tj = P.mma_tiles(32, 64)
+    na = int(P.scalars[0])
+    assert nptr[0] == 0 and nptr[-1] == na and np.all(np.diff(nptr) >= 1) and np.all(np.diff(nptr) <= 32)
+    assert np.all(np.diff(eptr) <= 64) and eptr[-1] == len(elist)
+    tptr, tlist = P.tptr, P.tlist
+    for t in range(len(nptr) - 1):
+        els = elist[eptr[t]:eptr[t + 1]]
+        assert len(set(els.tolist())) == len(els)
+        q0, q1 = tptr[nptr[t]], tptr[nptr[t + 1]]
+        assert np.array_equal(els[tj[q0:q1]], (tlist[q0:q1] >> 1) >> 2)
+    # a tile closes early instead of exceeding its element budget
+    nptr16, eptr16, _, _ = P.mma_tiles(32, 16)
+    assert np.all(np.diff(eptr16) <= 16) and nptr16[-1] == na
+
+
+def test_tensor_core_b_operand_is_the_q4_stiffness():
+    """The tensor-core step's B operand is [Kmu; Klambda] = [calck(1, 0);
+    calck(0, 1)] (formulation.f90:276-313; K is symmetric, so its rows are
+    its columns), split into tf32 hi and lo parts: both parts have a 10-bit
+    mantissa and hi + lo is the FP64 entry to 2^-21 relative."""
+    b = np.zeros(256, np.float32)
+    npb.lib().probe_mma_btile(b.ctypes.data_as(C.c_void_p))
+    bits = b.view(np.uint32)
+    assert np.all(bits & 0x1FFF == 0)
+
+    def at(tile, n, k):   # the K-major core-matrix layout of the operand tile
+        return tile[((n >> 3) * 256 + (k >> 2) * 128 + (n & 7) * 16 + (k & 3) * 4) // 4]
+
+    hi, lo = b[:128], b[128:]
+    for part, (mu, lam) in enumerate(((1.0, 0.0), (0.0, 1.0))):
+        K = oracle.calck(mu, lam)
+        for n in range(8):
+            for k in range(8):
+                got = float(at(hi, 8 * part + n, k)) + float(at(lo, 8 * part + n, k))
+                assert abs(got - K[n, k]) <= 2.0 ** -21 * max(abs(K[n, k]), 1e-30), (part, n, k, got, K[n, k])
