@@ -68,6 +68,8 @@ struct DevModel {
     int *d_step;             // steps completed (device counter)
     unsigned *d_blocks;      // last-block counter
     int *d_flag;             // watchdog flags
+    int *d_drm_step;         // FP32 side-stream DRM: the last step whose forces are computed
+    unsigned *d_drm_blocks;  // its last-block counter
 };
 
 struct Ctx {
@@ -115,6 +117,18 @@ struct Ctx {
     int pipe_grid = 0, pipe_threads = 0, pipe_nstage = 0;
     unsigned pipe_stage = 0;
     unsigned pipe_off[6] = {0, 0, 0, 0, 0, 0};   // D, D_comp, u_comp, node records, slots, coefficients
+    // FP32 form with few RHS: the next step's DRM forces run on a second stream
+    // (k_drm32) while this step's k_step32 runs, into the other of two force
+    // slots (see f32_launch_step)
+    bool drm_side = false;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_step = nullptr, ev_fork = nullptr, ev_drm[2] = {nullptr, nullptr};
+    // the events used while a graph is captured (an event last recorded in a
+    // capture cannot be waited on outside it)
+    cudaEvent_t cev_step = nullptr, cev_drm[2] = {nullptr, nullptr};
+    float *fdrm_slot[2] = {nullptr, nullptr};
+    bool drm_wait[2] = {false, false};   // a k_drm32 into slot s that the main stream has not waited for
+    bool ev_step_valid = false;          // ev_step marks the previous step's k_step32
     int parity = 0;          // index of the current u buffer
     int steps_done = 0;
     bool inited = false;
@@ -123,6 +137,7 @@ struct Ctx {
     int graph_steps = 0;
     int graph_parity = -1;
     int block_threads = 128;
+    int persist_grid = 0;    // FP32 variant 4: blocks of the persistent step grid (0 until the first launch)
     int rhs_per_thread = 1;
     bool idx32 = true;   // k_step32 with 32-bit indices (every index below 2^32)
     int num_sms = 1;     // SMs of the context's device
@@ -160,6 +175,12 @@ constexpr bool f32_term_corners(int R) { return R > 4; }
 // served requests; no gain at 64.
 constexpr bool f32_interleave(int R) { return R < 64; }
 
+// FP32 form: right-hand-side counts up to which the next step's DRM forces
+// run on a second stream beside the step (k_drm32) instead of inside the
+// hanging/receiver pass, where the latency of their FP64 chains holds up every
+// step of a mesh too small to hide it.
+constexpr int kDrmSideMaxRhs = 64;
+
 // Device memory of a context: a stream-ordered allocation on its stream from
 // the library's memory pool for the device, which keeps what destroyed
 // contexts freed for the next ones (no cudaMalloc, and no cudaFree, which
@@ -184,6 +205,9 @@ int f32_init(Ctx &c);
 int f32_tune_in_place(Ctx &c);
 int f32_launch_step(Ctx &c, int par);
 int f32_launch_sample0(Ctx &c, int par);
+// Makes the main stream wait for any side-stream DRM launch it has not
+// waited for (before a sync point, a graph replay or the end of a capture).
+int f32_join_side(Ctx &c);
 // bf16 <-> float on the host (round to nearest even), for tests and read-back.
 float bf16_to_float(unsigned short h);
 

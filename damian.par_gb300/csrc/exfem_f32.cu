@@ -317,6 +317,27 @@ __device__ __forceinline__ void drm32_items(const DevModel &m, int ipb, long lon
     m.fdrm32[((size_t)s * 8 + 2 * k) * m.R + row_off(m, 1, r)] = p[2 * k + 1];
 }
 
+// The DRM forces of the step after the last one computed (the side-stream
+// form): that step comes from the launch's own counter, which only these
+// launches advance (they run in order on one stream), not from the step
+// counter, which the main stream's hanging pass advances concurrently.
+// Writes m.fdrm32 (the slot the caller picked); the last block advances the
+// counter.
+__global__ void __launch_bounds__(256) k_drm32(DevModel m, int ipb) {
+    const int step = *(volatile int *)m.d_drm_step + 1;
+    drm32_items(m, ipb, blockIdx.x, step);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(m.d_drm_blocks, 1u);
+        if (prev == gridDim.x - 1) {
+            *m.d_drm_step = step;
+            *m.d_drm_blocks = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // Free-field delays of the DRM corners, once per context (see
 // planewave32_delays): thread per (DRM element, corner, rhs).
 __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
@@ -406,15 +427,15 @@ __device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R,
 // PAIR: the state is grouped by RPT (m.lg == RPT, row_off; with RPT == R
 // that is the plain layout), so the thread's x and y values of a node are
 // adjacent and load and store as one vector (XY).
-template <int RPT, bool I32, bool TC = true, bool PAIR = false>
-__global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
-                                                unsigned short *__restrict__ uc, float *__restrict__ dh,
-                                                unsigned short *__restrict__ dc) {
+template <int RPT, bool I32, bool TC, bool PAIR>
+__device__ __forceinline__ void step32_tile(const DevModel &m, unsigned tile, const float *__restrict__ uh,
+                                            float *__restrict__ uhn, unsigned short *__restrict__ uc,
+                                            float *__restrict__ dh, unsigned short *__restrict__ dc) {
     using I = typename std::conditional<I32, unsigned, size_t>::type;
     const int G = m.R / RPT;
     int n, r0;
     if (I32) {
-        const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+        const unsigned t = tile * blockDim.x + threadIdx.x;
         if (t >= (unsigned)m.n_active * (unsigned)G) return;
         if ((G & (G - 1)) == 0) {
             n = (int)(t >> (__ffs(G) - 1));
@@ -424,7 +445,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
             r0 = (int)(t % (unsigned)G) * RPT;
         }
     } else {
-        const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+        const long long t = (long long)tile * blockDim.x + threadIdx.x;
         if (t >= (long long)m.n_active * G) return;
         n = (int)(t / G);
         r0 = (int)(t % G) * RPT;
@@ -446,7 +467,7 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
     // either form: measured the same with per-thread, bulk or no prefetches.
     if ((m.R & 3) == 0) {
         if (threadIdx.x == 0) {
-            const long long tb = (long long)blockIdx.x * blockDim.x;
+            const long long tb = (long long)tile * blockDim.x;
             const int na = (int)(tb / G);
             const int nz = (int)min((long long)m.n_active, (tb + blockDim.x - 1) / G + 1);
             const size_t e0 = (size_t)na * 2 * m.R, cnt = (size_t)(nz - na) * 2 * m.R;
@@ -506,6 +527,24 @@ __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restr
         }
     }
     node_update<RPT, PAIR, I>(m, n, bn, R, roff, ax, ay, uh, uhn, uc, dh, dc);
+}
+
+template <int RPT, bool I32, bool TC = true, bool PAIR = false>
+__global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
+                                                unsigned short *__restrict__ uc, float *__restrict__ dh,
+                                                unsigned short *__restrict__ dc) {
+    step32_tile<RPT, I32, TC, PAIR>(m, blockIdx.x, uh, uhn, uc, dh, dc);
+}
+
+// The same step as a persistent kernel (variant 4): a grid of as many blocks
+// as fit on the device at once, each striding over the block-sized tiles of
+// (node, RHS group) threads that k_step32 gives one block each.
+template <int RPT, bool I32, bool TC = true, bool PAIR = false>
+__global__ void __launch_bounds__(512) k_step32p(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
+                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
+                                                 unsigned short *__restrict__ dc, unsigned ntiles) {
+    for (unsigned tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+        step32_tile<RPT, I32, TC, PAIR>(m, tile, uh, uhn, uc, dh, dc);
 }
 
 // Tiled variant of k_step32: a block owns `tn` consecutive active nodes (a
@@ -1240,6 +1279,9 @@ __global__ void __launch_bounds__(256) k_hang32(DevModel m, const float *__restr
                                                 unsigned short *__restrict__ dc, int nb_hang, int mode, int ipb,
                                                 int nb_recv, int ipb_drm) {
     int step = (mode == 1) ? 0 : read_step(m) + 1;
+    // the step-0 sample computes step 1's DRM forces: the side-stream DRM
+    // launches continue from there
+    if (mode == 1 && blockIdx.x == 0 && threadIdx.x == 0) *m.d_drm_step = 1;
     // the DRM blocks, whose FP64/exp chains are the longest, take the lowest
     // block indices so that they are scheduled first
     const int nb_drm = (int)gridDim.x - nb_hang - nb_recv;
@@ -1504,7 +1546,19 @@ int f32_alloc(Ctx &c) {
     if ((rc = upload32(c, nc, &m.ncoef4))) return rc;
     if ((rc = upload32(c, hc, &m.hcoef4))) return rc;
     if ((rc = upload32(c, P.ecoef32, &m.ecoef32))) return rc;
-    if ((rc = alloc32(c, (size_t)std::max(m.ns, 1) * 8 * P.R, &m.fdrm32))) return rc;
+    // with few right-hand sides the next step's DRM forces run beside this
+    // step on a second stream, into the other of two force slots
+    c.drm_side = m.ns > 0 && P.R <= kDrmSideMaxRhs && c.opts.drm_inline == 0;
+    const size_t slot = (size_t)std::max(m.ns, 1) * 8 * P.R;
+    if ((rc = alloc32(c, slot * (c.drm_side ? 2 : 1), &m.fdrm32))) return rc;
+    if (c.drm_side) {
+        c.fdrm_slot[0] = m.fdrm32;
+        c.fdrm_slot[1] = m.fdrm32 + slot;
+        CK(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+        for (cudaEvent_t *e : {&c.ev_step, &c.ev_fork, &c.ev_drm[0], &c.ev_drm[1], &c.cev_step, &c.cev_drm[0],
+                               &c.cev_drm[1]})
+            CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    }
     m.drm_delay = nullptr;
     if (m.ns > 0) {
         double *dd = nullptr;
@@ -1553,7 +1607,8 @@ int f32_alloc(Ctx &c) {
     // default block: 256, and 128 for the direct gather from four RHS
     // (measured on 0.1M- and 0.55M-element valleys: 1-3% faster than 256 on
     // the larger mesh, within 2% either way on the smaller)
-    if (c.opts.block_threads <= 0) c.block_threads = (P.R >= 4 && c.opts.variant == 0) ? 128 : 256;
+    if (c.opts.block_threads <= 0)
+        c.block_threads = (P.R >= 4 && (c.opts.variant == 0 || c.opts.variant == 4)) ? 128 : 256;
     // shared-memory tiles (variant 1; variant 0, the default, is the direct gather)
     c.use_tiles = false;
     if (c.opts.variant == 1) {
@@ -1657,7 +1712,7 @@ int f32_tune_in_place(Ctx &c) {
         for (int bt : {128, 256, 512}) {
             f32_set_shape(c, rpt, bt);
             if ((rc = f32_init(c))) break;
-            if (cudaMemsetAsync(c.dm.d_step, 0, 4 * sizeof(int), c.stream) != cudaSuccess) { rc = EXFEM_E_CUDA; break; }
+            if (cudaMemsetAsync(c.dm.d_step, 0, 8 * sizeof(int), c.stream) != cudaSuccess) { rc = EXFEM_E_CUDA; break; }
             int par = 0;
             if ((rc = f32_launch_step(c, par))) break;   // warm-up step
             par ^= 1;
@@ -1666,6 +1721,7 @@ int f32_tune_in_place(Ctx &c) {
                 rc = f32_launch_step(c, par);
                 par ^= 1;
             }
+            if (!rc) rc = f32_join_side(c);   // the side stream is idle before the next shape resets the counters
             cudaEventRecord(b, c.stream);
             float ms = 0.f;
             if (rc || cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
@@ -1704,16 +1760,65 @@ int f32_init(Ctx &c) {
 
 // k_step32 with 32- or 64-bit indices as the context allows.
 template <int RPT, bool TC, bool PAIR>
-static void step32(Ctx &c, int nb, int T, const float *uh, float *uhn) {
-    if (c.idx32) k_step32<RPT, true, TC, PAIR><<<nb, T, 0, c.stream>>>(c.dm, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-    else k_step32<RPT, false, TC, PAIR><<<nb, T, 0, c.stream>>>(c.dm, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+static void step32(Ctx &c, const DevModel &m, int nb, int T, const float *uh, float *uhn) {
+    if (c.opts.variant == 4) {   // persistent: the blocks that fit at once stride over the tiles
+        if (c.persist_grid <= 0) {
+            int per = 0;
+            if (c.idx32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step32p<RPT, true, TC, PAIR>, T, 0);
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step32p<RPT, false, TC, PAIR>, T, 0);
+            c.persist_grid = std::max(1, per) * c.num_sms;
+        }
+        const int g = std::min(nb, c.persist_grid);
+        if (c.idx32)
+            k_step32p<RPT, true, TC, PAIR><<<g, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, (unsigned)nb);
+        else
+            k_step32p<RPT, false, TC, PAIR><<<g, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, (unsigned)nb);
+        return;
+    }
+    if (c.idx32) k_step32<RPT, true, TC, PAIR><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+    else k_step32<RPT, false, TC, PAIR><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+}
+
+int f32_join_side(Ctx &c) {
+    for (int s = 0; s < 2; ++s)
+        if (c.drm_wait[s]) {
+            CK(cudaStreamWaitEvent(c.stream, c.ev_drm[s], 0));
+            c.drm_wait[s] = false;
+        }
+    return EXFEM_OK;
 }
 
 int f32_launch_step(Ctx &c, int par) {
-    DevModel &m = c.dm;
+    DevModel m = c.dm;
     float *uh = c.uhi[par], *uhn = c.uhi[par ^ 1];
-    // (this step's DRM forces came from the previous step's k_hang32, or for
-    // step 1 from the step-0 sample)
+    // This step's DRM forces came from the previous step's k_hang32 (or for
+    // step 1 from the step-0 sample).  With few RHS they come instead from a
+    // k_drm32 on the side stream, into slot `par` of two: step k reads slot
+    // (k - 1) & 1, and while it runs the side stream computes step k + 1's
+    // forces into the other slot, once step k - 1 (which read that slot) is
+    // done.  Under exfem_gpu_profile_kernels it runs on the main stream, so the
+    // per-launch marks time it alone.
+    if (c.drm_side) {
+        m.fdrm32 = c.fdrm_slot[par];
+        if (c.drm_wait[par]) {
+            CK(cudaStreamWaitEvent(c.stream, c.ev_drm[par], 0));
+            c.drm_wait[par] = false;
+        }
+        DevModel md = c.dm;
+        md.fdrm32 = c.fdrm_slot[par ^ 1];
+        const long long WD = (long long)md.ns * md.R;   // four threads per (DRM element, rhs)
+        const int ipd = spread_per_block(WD, c.num_sms, 64);
+        if (c.prof_on) {
+            k_drm32<<<spread_blocks(WD, ipd), 256, 0, c.stream>>>(md, ipd);
+            mark(c, "k_drm32");
+        } else {
+            if (c.ev_step_valid) CK(cudaStreamWaitEvent(c.side, c.ev_step, 0));
+            k_drm32<<<spread_blocks(WD, ipd), 256, 0, c.side>>>(md, ipd);
+            CK(cudaEventRecord(c.ev_drm[par ^ 1], c.side));
+            c.drm_wait[par ^ 1] = true;
+        }
+        c.launches++;
+    }
     const int T = c.block_threads;
     const int rpt = c.rhs_per_thread;
     long long work = (long long)m.n_active * (m.R / rpt);
@@ -1763,28 +1868,32 @@ int f32_launch_step(Ctx &c, int par) {
             return EXFEM_E_STATE;
         }
         switch (rpt) {
-            case 4: step32<4, false, true>(c, nb, T, uh, uhn); break;
-            case 2: step32<2, false, true>(c, nb, T, uh, uhn); break;
-            default: step32<1, false, true>(c, nb, T, uh, uhn); break;
+            case 4: step32<4, false, true>(c, m, nb, T, uh, uhn); break;
+            case 2: step32<2, false, true>(c, m, nb, T, uh, uhn); break;
+            default: step32<1, false, true>(c, m, nb, T, uh, uhn); break;
         }
     } else {
         switch (rpt) {
             case 4:
-                if (pair) step32<4, true, true>(c, nb, T, uh, uhn);
-                else step32<4, true, false>(c, nb, T, uh, uhn);
+                if (pair) step32<4, true, true>(c, m, nb, T, uh, uhn);
+                else step32<4, true, false>(c, m, nb, T, uh, uhn);
                 break;
             case 2:
-                if (pair) step32<2, true, true>(c, nb, T, uh, uhn);
-                else step32<2, true, false>(c, nb, T, uh, uhn);
+                if (pair) step32<2, true, true>(c, m, nb, T, uh, uhn);
+                else step32<2, true, false>(c, m, nb, T, uh, uhn);
                 break;
             default:
-                if (pair) step32<1, true, true>(c, nb, T, uh, uhn);
-                else step32<1, true, false>(c, nb, T, uh, uhn);
+                if (pair) step32<1, true, true>(c, m, nb, T, uh, uhn);
+                else step32<1, true, false>(c, m, nb, T, uh, uhn);
                 break;
         }
     }
     c.launches++;
-    mark(c, "k_step32");
+    mark(c, c.opts.variant == 4 ? "k_step32p" : "k_step32");
+    }
+    if (c.drm_side && !c.prof_on) {   // the side stream's next launch may overwrite the slot this step read
+        CK(cudaEventRecord(c.ev_step, c.stream));
+        c.ev_step_valid = true;
     }
     if (c.p32_n > 0) {
         k_point32<<<nblocks((long long)c.p32_n * m.R, 128), 128, 0, c.stream>>>(m, c.p32_node, c.p32_w, c.p32_n, uhn,
@@ -1797,7 +1906,7 @@ int f32_launch_step(Ctx &c, int par) {
     const long long WR = (long long)m.nrecv * m.R;   // four threads per (receiver, rhs)
     const int ipb = spread_per_block(WR, c.num_sms, TH / 4);
     const int nbr = WR > 0 ? spread_blocks(WR, ipb) : 0;
-    const long long WD = (long long)m.ns * m.R;      // four threads per (DRM element, rhs)
+    const long long WD = c.drm_side ? 0 : (long long)m.ns * m.R;   // four threads per (DRM element, rhs)
     const int ipd = spread_per_block(WD, c.num_sms, TH / 4);
     const int nbd = WD > 0 ? spread_blocks(WD, ipd) : 0;
     k_hang32<<<nbh + nbr + nbd, TH, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, nbh, 0, ipb, nbr, ipd);
@@ -1808,7 +1917,10 @@ int f32_launch_step(Ctx &c, int par) {
 }
 
 int f32_launch_sample0(Ctx &c, int par) {
-    DevModel &m = c.dm;
+    DevModel m = c.dm;
+    if (c.drm_side) m.fdrm32 = c.fdrm_slot[0];   // step 1 reads slot 0
+    c.drm_wait[0] = c.drm_wait[1] = false;
+    c.ev_step_valid = false;
     const int TH = 256;
     const long long WR = (long long)m.nrecv * m.R;   // four threads per (receiver, rhs)
     const int ipb = spread_per_block(WR, c.num_sms, TH / 4);

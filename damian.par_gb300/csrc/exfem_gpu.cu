@@ -387,10 +387,12 @@ int setup_device(Ctx &c) {
     TRY(dalloc(c, (size_t)std::max(m.ns, 1) * 16 * P.R, &m.fdrm));
     TRY(dalloc(c, (size_t)P.R * P.nsave * std::max(P.nrecv, 1) * 2, &m.seis));
     int *ctr = nullptr;
-    TRY(dalloc(c, 4, &ctr));
+    TRY(dalloc(c, 8, &ctr));
     m.d_step = ctr;
     m.d_flag = ctr + 1;
     m.d_blocks = reinterpret_cast<unsigned *>(ctr + 2);
+    m.d_drm_step = ctr + 3;
+    m.d_drm_blocks = reinterpret_cast<unsigned *>(ctr + 4);
     return EXFEM_OK;
 }
 
@@ -405,6 +407,14 @@ int alloc_fp64(Ctx &c) {
 
 void free_all(Ctx &c) {
     if (c.graph) { cudaGraphExecDestroy(c.graph); c.graph = nullptr; }
+    if (c.side) {
+        cudaStreamSynchronize(c.side);
+        cudaStreamDestroy(c.side);
+        c.side = nullptr;
+    }
+    for (cudaEvent_t *e : {&c.ev_step, &c.ev_fork, &c.ev_drm[0], &c.ev_drm[1], &c.cev_step, &c.cev_drm[0],
+                           &c.cev_drm[1]})
+        if (*e) { cudaEventDestroy(*e); *e = nullptr; }
     if (c.stream) {
         for (void *p : c.allocs) cudaFreeAsync(p, c.stream);   // back to the pool, in stream order
         cudaStreamSynchronize(c.stream);
@@ -424,12 +434,39 @@ int capture_graph(Ctx &c, int g) {
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
     long long before = c.launches;
-    int par = 0, rc = EXFEM_OK;
+    // The side stream (FP32 DRM forces) joins the capture through an event of
+    // the main stream and rejoins it at the end.  Inside the graph the first
+    // step waits for no earlier DRM launch: a replay starts only after the
+    // host has made the main stream wait for them (f32_join_side).
+    const bool w0 = c.drm_wait[0], w1 = c.drm_wait[1], sv = c.ev_step_valid;
+    int rc = EXFEM_OK;
+    if (c.drm_side) {
+        cudaEventRecord(c.ev_fork, c.stream);
+        cudaStreamWaitEvent(c.side, c.ev_fork, 0);
+        c.drm_wait[0] = c.drm_wait[1] = false;
+        c.ev_step_valid = false;
+        std::swap(c.ev_step, c.cev_step);
+        std::swap(c.ev_drm[0], c.cev_drm[0]);
+        std::swap(c.ev_drm[1], c.cev_drm[1]);
+    }
+    int par = 0;
     for (int i = 0; i < g && rc == EXFEM_OK; ++i) {
         rc = launch_step(c, par);
         par ^= 1;
     }
+    if (c.drm_side) {
+        const int rj = f32_join_side(c);
+        if (!rc) rc = rj;
+    }
     cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
+    if (c.drm_side) {
+        std::swap(c.ev_step, c.cev_step);
+        std::swap(c.ev_drm[0], c.cev_drm[0]);
+        std::swap(c.ev_drm[1], c.cev_drm[1]);
+    }
+    c.drm_wait[0] = w0;
+    c.drm_wait[1] = w1;
+    c.ev_step_valid = sv;
     c.launches = before;   // captured launches are counted on replay
     if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
     if (e != cudaSuccess) { c.err = std::string("graph capture: ") + cudaGetErrorString(e); return EXFEM_E_CUDA; }
@@ -445,7 +482,7 @@ int launches_per_step(const Ctx &c) {
     // step's DRM forces inside their hanging/receiver kernel
     if (c.precision == EXFEM_FP64)
         return (c.dm.ns > 0 && c.opts.variant != EXFEM_VARIANT_REFERENCE_ORDER ? 1 : 0) + 3;   // (drm,) elem, node, hang
-    return 2 + (c.p32_n > 0 ? 1 : 0);   // step, (point,) hang
+    return 2 + (c.p32_n > 0 ? 1 : 0) + (c.drm_side ? 1 : 0);   // step, (point,) hang, (side-stream DRM)
 }
 
 // Device side of exfem_gpu_create: stream, uploads, state buffers.
@@ -550,6 +587,7 @@ void exfem_gpu_default_opts(exfem_opts *o) {
     o->pad_rhs = 0;
     o->wait_cycles = 0;
     o->tune = 0;
+    o->drm_inline = 0;
 }
 
 int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts, exfem_ctx **out) {
@@ -560,7 +598,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     if (opts) o = *opts;
     else exfem_gpu_default_opts(&o);
     if (o.precision != EXFEM_FP64 && o.precision != EXFEM_FP32_KAHAN) { g_create_err = "unknown precision"; return EXFEM_E_ARG; }
-    if (o.variant < 0 || o.variant > (o.precision == EXFEM_FP32_KAHAN ? 3 : 1)) {
+    if (o.variant < 0 || o.variant > (o.precision == EXFEM_FP32_KAHAN ? 4 : 1)) {
         g_create_err = "unknown kernel variant";
         return EXFEM_E_ARG;
     }
@@ -568,6 +606,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     if (o.pad_rhs != 0 && o.pad_rhs != 1) { g_create_err = "pad_rhs must be 0 or 1"; return EXFEM_E_ARG; }
     if (o.wait_cycles < 0) { g_create_err = "wait_cycles must be >= 0"; return EXFEM_E_ARG; }
     if (o.tune != 0 && o.tune != 1) { g_create_err = "tune must be 0 or 1"; return EXFEM_E_ARG; }
+    if (o.drm_inline != 0 && o.drm_inline != 1) { g_create_err = "drm_inline must be 0 or 1"; return EXFEM_E_ARG; }
     const int max_bt = o.precision == EXFEM_FP64 ? 256 : 512;   // the kernels' __launch_bounds__
     if (o.block_threads < 0 || o.block_threads > max_bt || (o.block_threads % 32) != 0) {
         g_create_err = "block_threads must be a multiple of 32 in [0, " + std::to_string(max_bt) + "]";
@@ -628,7 +667,7 @@ int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out) {
     }
     CK(cudaMemsetAsync(m.seis, 0, sizeof(double) * (size_t)c.plan.R * c.plan.nsave * std::max(c.plan.nrecv, 1) * 2,
                        c.stream));
-    CK(cudaMemsetAsync(m.d_step, 0, 4 * sizeof(int), c.stream));
+    CK(cudaMemsetAsync(m.d_step, 0, 8 * sizeof(int), c.stream));
     c.parity = 0;
     c.steps_done = 0;
     int rc = c.precision == EXFEM_FP64 ? launch_sample0_64(c, 0) : f32_launch_sample0(c, 0);
@@ -665,7 +704,15 @@ int exfem_gpu_run(exfem_ctx *ctx, int nsteps) {
                 c.steps_done++;
             }
             while (left >= g) {
+                if (c.drm_side) {
+                    int rj = f32_join_side(c);
+                    if (rj) return rj;
+                }
                 CK(cudaGraphLaunch(c.graph, c.stream));
+                if (c.drm_side) {   // the replay joined its side work; later side launches follow it
+                    CK(cudaEventRecord(c.ev_step, c.stream));
+                    c.ev_step_valid = true;
+                }
                 c.launches += (long long)g * launches_per_step(c);
                 left -= g;
                 c.steps_done += g;
@@ -679,7 +726,8 @@ int exfem_gpu_run(exfem_ctx *ctx, int nsteps) {
         --left;
         c.steps_done++;
     }
-    return EXFEM_OK;
+    // the main stream covers the last side-stream launch (sync, query, events)
+    return c.drm_side ? f32_join_side(c) : EXFEM_OK;
 }
 
 int exfem_gpu_sync(exfem_ctx *ctx) {
@@ -911,7 +959,7 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
     b += 16 * std::max(ns, (size_t)1) * R * 8;                      // DRM forces
     b += R * nsave * std::max(nr, (size_t)1) * 16 + 16;            // seismograms, counters
     if (f64) b += R * (nn * 32 + ne * 64);                          // u ping-pong, element forces
-    else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 32 * std::max(ns, (size_t)1) * R + 96 * ns * R +
+    else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 64 * std::max(ns, (size_t)1) * R + 96 * ns * R +
               R * nn * 2 * (4 + 4 + 2 + 4 + 2);                     // FP32 state
     if (!f64 && opts->variant >= 1) {
         // tiles: every halo entry is a node or a corner/anchor of one of its terms

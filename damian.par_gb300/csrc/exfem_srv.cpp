@@ -271,6 +271,8 @@ void exfem_srv_default_opts(exfem_srv_opts *o) {
     o->max_bypass = 8;
     exfem_gpu_default_opts(&o->solver);
     o->solver.precision = EXFEM_FP32_KAHAN;
+    // requests stepping at once hide each other's DRM pass: no second stream
+    o->solver.drm_inline = 1;
 }
 
 int exfem_srv_open(const exfem_srv_opts *opts, exfem_srv **out) {

@@ -1,9 +1,10 @@
 // exfem_tune.cpp — the autotuner of the FP32 step (exfem_gpu_autotune).
 //
 // It times every candidate shape of the FP32 form on the caller's own model
-// and keeps the fastest: kernel variant (0 direct gather, 1 shared-memory
-// tiles, 2 bulk-copy pipeline when nrhs is a multiple of 4, 3 tensor-core
-// step when nrhs is a multiple of 16), block size (128, 256, 512) and
+// and keeps the fastest: kernel variant (0 direct gather, 4 the same as a
+// persistent grid, 1 shared-memory tiles, 2 bulk-copy pipeline when nrhs is
+// a multiple of 4, 3 tensor-core step when nrhs is a multiple of 16), block
+// size (128, 256, 512) and
 // right-hand sides per thread (1, 2, 4 dividing nrhs).
 // Each candidate gets its own context (exfem_gpu_create with that shape), a
 // few warm-up steps, and a burst timed with CUDA events on the context's
@@ -82,7 +83,7 @@ int autotune_shapes(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opt
     exfem_problem p = *prob;   // enough steps for the timing, whatever the problem's length
     p.nsteps = warmup + steps;
     if (p.io_interval < 1) p.io_interval = 1;
-    std::vector<int> variants = {0};
+    std::vector<int> variants = {0, 4};
     if (max_variant >= 1) variants.push_back(1);
     if (max_variant >= 2 && R % 4 == 0) variants.push_back(2);
     if (max_variant >= 3 && R % 16 == 0) variants.push_back(3);

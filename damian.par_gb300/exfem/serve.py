@@ -40,7 +40,7 @@ class Server:
         o.chunk_steps = int(chunk_steps)
         o.preparers = int(preparers)
         o.max_bypass = int(max_bypass)
-        so = default_opts(**{"precision": 1, **solver_opts})
+        so = default_opts(**{"precision": 1, "drm_inline": 1, **solver_opts})
         o.solver = so
         h = C.c_void_p()
         rc = L.exfem_srv_open(C.byref(o), C.byref(h))

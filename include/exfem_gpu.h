@@ -136,9 +136,9 @@ typedef struct exfem_opts {
                           shared-memory pipeline (persistent grid; needs nrhs
                           a multiple of 4, else the direct gather runs),
                           3 = element products on the tensor cores (tcgen05
-                          kind::tf32 in 3xTF32; needs nrhs a multiple of 16
-                          and at most 64 elements per 32-node tile, else the
-                          direct gather runs)                               */
+                          kind::tf32 in 3xTF32; needs nrhs a multiple of 16,
+                          else the direct gather runs), 4 = the direct
+                          gather as a persistent grid (same results as 0)  */
     int index_bits;    /* FP32 direct gather: 0 = 32-bit indices when every
                           thread id and array index fits, else 64; 64 = always
                           64-bit (same results)                               */
@@ -163,6 +163,15 @@ typedef struct exfem_opts {
                           unless rhs_per_thread or block_threads is set; the
                           state is then reset.  0 = the built-in choice.
                           Same results either way                         */
+    int drm_inline;    /* FP32 form: 0 = the next step's DRM forces run on a
+                          second stream beside the step kernel, into the
+                          other of two force slots (default; a context
+                          stepping alone: 4-20% less time per step on the
+                          canyons and valleys of 1-16 RHS); 1 = inside the
+                          hanging/receiver pass (the server's default: with
+                          many requests stepping at once their kernels hide
+                          that pass anyway, and the second streams measured
+                          3% slower on a saturated burst).  Same results   */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;
@@ -275,9 +284,9 @@ int exfem_gpu_step_noalloc(exfem_ctx *ctx, int step, const double *d_u, const do
 
 /* Autotuner of the FP32 form (opts->precision must be EXFEM_FP32_KAHAN).
  * Times every candidate shape on this mesh and problem and writes the
- * fastest into opts: variant (0 direct gather, 1 shared-memory tiles, 2
- * bulk-copy pipeline when the right-hand sides are a multiple of 4, 3
- * tensor-core step when they are a multiple of 16),
+ * fastest into opts: variant (0 direct gather, 4 the same as a persistent
+ * grid, 1 shared-memory tiles, 2 bulk-copy pipeline when the right-hand sides
+ * are a multiple of 4, 3 tensor-core step when they are a multiple of 16),
  * block_threads (128, 256, 512) and rhs_per_thread (1, 2, 4).  Each
  * candidate runs in a context of its own (one at a time: the device must
  * hold one more context of this problem), 3 warm-up steps and `steps` steps

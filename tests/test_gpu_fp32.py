@@ -131,7 +131,7 @@ def test_autotuner_picks_a_working_shape():
     m = workloads.build("valley_batched", scale=0.1, steps=40)
     choice = autotune.tune(m, steps=8)
     assert choice["rhs_per_thread"] in (1, 2, 4) and choice["block_threads"] in (128, 256, 512)
-    assert choice["variant"] in (0, 1, 2) and choice["ms_per_step"] > 0
+    assert choice["variant"] in (0, 1, 2, 3, 4) and choice["ms_per_step"] > 0
     t0 = time.perf_counter()
     again = autotune.tune(m, steps=8)
     assert time.perf_counter() - t0 < 0.05 and again == choice
@@ -414,3 +414,44 @@ def test_tensor_core_step_runs_and_matches_the_direct_gather():
         s.init_explicit()
         names = s.kernel_times(2)
     assert "k_step32" in names and "k_mma32" not in names, names
+
+
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_side_stream_drm_forces_match_the_inline_pass(use_graph):
+    """exfem_opts.drm_inline = 0 (the default) computes the next step's DRM
+    forces on a second stream while the step runs, into the other of two
+    force slots; = 1 computes them inside the hanging/receiver pass.  Both
+    evaluate the same forces for the same steps: seismograms and state are
+    the same bit for bit, with graph replays mixed with single steps (the
+    host's joins before replays and at the end of each run) and without
+    graphs, on a refined canyon with 8 RHS and on the 64-RHS valley."""
+    for m in (workloads.build("canyon", scale=0.2, steps=130, save_every=1, waves=EIGHT_WAVES),
+              workloads.build("valley_batched", scale=0.08, steps=130, save_every=2)):
+        runs = []
+        for inline in (1, 0):
+            with Solver(m, precision=EXFEM_FP32_KAHAN, drm_inline=inline, use_graph=use_graph) as s:
+                s.init_explicit()
+                for n in (1, 17, 40, 72):
+                    s.run(n)
+                s.sync()
+                runs.append((s.seismograms(), [s.u(r) for r in range(s.nrhs)]))
+        assert np.array_equal(runs[0][0], runs[1][0])
+        for r in range(m.problem.nrhs):
+            assert np.array_equal(runs[0][1][r], runs[1][1][r]), r
+
+
+def test_persistent_step_matches_the_direct_gather():
+    """Variant 4 runs the direct gather as a persistent grid (k_step32p: the
+    blocks that fit at once stride over the tiles); it computes the same
+    terms in the same order, so results are bit for bit those of variant 0."""
+    for m in (workloads.build("canyon", scale=0.2, steps=80, save_every=2, waves=EIGHT_WAVES),
+              workloads.build("valley_batched", scale=0.08, steps=80, save_every=2)):
+        with Solver(m, precision=EXFEM_FP32_KAHAN, variant=4) as s:
+            s.init_explicit()
+            names = s.kernel_times(2)
+        assert "k_step32p" in names and "k_step32" not in names, names
+        a, ua = run32(m, variant=0)
+        b, ub = run32(m, variant=4)
+        assert np.array_equal(a, b)
+        for r in range(m.problem.nrhs):
+            assert np.array_equal(ua[r], ub[r]), r
