@@ -117,9 +117,9 @@ struct Ctx {
     int pipe_grid = 0, pipe_threads = 0, pipe_nstage = 0;
     unsigned pipe_stage = 0;
     unsigned pipe_off[6] = {0, 0, 0, 0, 0, 0};   // D, D_comp, u_comp, node records, slots, coefficients
-    // FP32 form with few RHS: the next step's DRM forces run on a second stream
-    // (k_drm32) while this step's k_step32 runs, into the other of two force
-    // slots (see f32_launch_step)
+    // The next step's DRM forces on a second stream (k_drm32 in the FP32
+    // form, k_drm_ref_side in the reference-order FP64 form) while this step
+    // runs, into the other of two force slots (see side_drm_next)
     bool drm_side = false;
     cudaStream_t side = nullptr;
     cudaEvent_t ev_step = nullptr, ev_fork = nullptr, ev_drm[2] = {nullptr, nullptr};
@@ -127,6 +127,7 @@ struct Ctx {
     // capture cannot be waited on outside it)
     cudaEvent_t cev_step = nullptr, cev_drm[2] = {nullptr, nullptr};
     float *fdrm_slot[2] = {nullptr, nullptr};
+    double *fdrm64_slot[2] = {nullptr, nullptr};
     bool drm_wait[2] = {false, false};   // a k_drm32 into slot s that the main stream has not waited for
     bool ev_step_valid = false;          // ev_step marks the previous step's k_step32
     int parity = 0;          // index of the current u buffer
@@ -205,9 +206,34 @@ int f32_init(Ctx &c);
 int f32_tune_in_place(Ctx &c);
 int f32_launch_step(Ctx &c, int par);
 int f32_launch_sample0(Ctx &c, int par);
-// Makes the main stream wait for any side-stream DRM launch it has not
+// Side-stream DRM forces, shared by both forms.  side_create makes the
+// stream and events.  side_drm_next, before step k's kernels (at parity
+// `par`): makes the main stream wait for step k's forces (slot par) if a
+// side launch made them, then queues `launch(stream)` for step k + 1's forces
+// into slot par ^ 1 on the side stream, after step k - 1's reader of that
+// slot (the main stream under exfem_gpu_profile_kernels, which times each
+// launch alone).  side_mark, after the last kernel of step k that reads its
+// slot.  side_join makes the main stream wait for any side launch it has not
 // waited for (before a sync point, a graph replay or the end of a capture).
-int f32_join_side(Ctx &c);
+int side_create(Ctx &c);
+template <class F>
+int side_drm_next(Ctx &c, int par, F &&launch) {
+    if (c.drm_wait[par]) {
+        if (cudaStreamWaitEvent(c.stream, c.ev_drm[par], 0) != cudaSuccess) return EXFEM_E_CUDA;
+        c.drm_wait[par] = false;
+    }
+    if (c.prof_on) {
+        launch(c.stream);
+        return EXFEM_OK;
+    }
+    if (c.ev_step_valid && cudaStreamWaitEvent(c.side, c.ev_step, 0) != cudaSuccess) return EXFEM_E_CUDA;
+    launch(c.side);
+    if (cudaEventRecord(c.ev_drm[par ^ 1], c.side) != cudaSuccess) return EXFEM_E_CUDA;
+    c.drm_wait[par ^ 1] = true;
+    return EXFEM_OK;
+}
+int side_mark(Ctx &c);
+int side_join(Ctx &c);
 // bf16 <-> float on the host (round to nearest even), for tests and read-back.
 float bf16_to_float(unsigned short h);
 

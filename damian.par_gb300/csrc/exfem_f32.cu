@@ -1554,10 +1554,7 @@ int f32_alloc(Ctx &c) {
     if (c.drm_side) {
         c.fdrm_slot[0] = m.fdrm32;
         c.fdrm_slot[1] = m.fdrm32 + slot;
-        CK(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
-        for (cudaEvent_t *e : {&c.ev_step, &c.ev_fork, &c.ev_drm[0], &c.ev_drm[1], &c.cev_step, &c.cev_drm[0],
-                               &c.cev_drm[1]})
-            CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        if ((rc = side_create(c))) return rc;
     }
     m.drm_delay = nullptr;
     if (m.ns > 0) {
@@ -1713,6 +1710,7 @@ int f32_tune_in_place(Ctx &c) {
             f32_set_shape(c, rpt, bt);
             if ((rc = f32_init(c))) break;
             if (cudaMemsetAsync(c.dm.d_step, 0, 8 * sizeof(int), c.stream) != cudaSuccess) { rc = EXFEM_E_CUDA; break; }
+            if (c.drm_side && (rc = side_mark(c))) break;   // side launches follow the reset
             int par = 0;
             if ((rc = f32_launch_step(c, par))) break;   // warm-up step
             par ^= 1;
@@ -1721,7 +1719,7 @@ int f32_tune_in_place(Ctx &c) {
                 rc = f32_launch_step(c, par);
                 par ^= 1;
             }
-            if (!rc) rc = f32_join_side(c);   // the side stream is idle before the next shape resets the counters
+            if (!rc) rc = side_join(c);   // the side stream is idle before the next shape resets the counters
             cudaEventRecord(b, c.stream);
             float ms = 0.f;
             if (rc || cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
@@ -1779,15 +1777,6 @@ static void step32(Ctx &c, const DevModel &m, int nb, int T, const float *uh, fl
     else k_step32<RPT, false, TC, PAIR><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
 }
 
-int f32_join_side(Ctx &c) {
-    for (int s = 0; s < 2; ++s)
-        if (c.drm_wait[s]) {
-            CK(cudaStreamWaitEvent(c.stream, c.ev_drm[s], 0));
-            c.drm_wait[s] = false;
-        }
-    return EXFEM_OK;
-}
-
 int f32_launch_step(Ctx &c, int par) {
     DevModel m = c.dm;
     float *uh = c.uhi[par], *uhn = c.uhi[par ^ 1];
@@ -1800,23 +1789,15 @@ int f32_launch_step(Ctx &c, int par) {
     // per-launch marks time it alone.
     if (c.drm_side) {
         m.fdrm32 = c.fdrm_slot[par];
-        if (c.drm_wait[par]) {
-            CK(cudaStreamWaitEvent(c.stream, c.ev_drm[par], 0));
-            c.drm_wait[par] = false;
-        }
         DevModel md = c.dm;
         md.fdrm32 = c.fdrm_slot[par ^ 1];
         const long long WD = (long long)md.ns * md.R;   // four threads per (DRM element, rhs)
         const int ipd = spread_per_block(WD, c.num_sms, 64);
-        if (c.prof_on) {
-            k_drm32<<<spread_blocks(WD, ipd), 256, 0, c.stream>>>(md, ipd);
+        const int rc = side_drm_next(c, par, [&](cudaStream_t st) {
+            k_drm32<<<spread_blocks(WD, ipd), 256, 0, st>>>(md, ipd);
             mark(c, "k_drm32");
-        } else {
-            if (c.ev_step_valid) CK(cudaStreamWaitEvent(c.side, c.ev_step, 0));
-            k_drm32<<<spread_blocks(WD, ipd), 256, 0, c.side>>>(md, ipd);
-            CK(cudaEventRecord(c.ev_drm[par ^ 1], c.side));
-            c.drm_wait[par ^ 1] = true;
-        }
+        });
+        if (rc) { c.err = "side-stream DRM launch failed"; return rc; }
         c.launches++;
     }
     const int T = c.block_threads;
@@ -1891,9 +1872,9 @@ int f32_launch_step(Ctx &c, int par) {
     c.launches++;
     mark(c, c.opts.variant == 4 ? "k_step32p" : "k_step32");
     }
-    if (c.drm_side && !c.prof_on) {   // the side stream's next launch may overwrite the slot this step read
-        CK(cudaEventRecord(c.ev_step, c.stream));
-        c.ev_step_valid = true;
+    if (c.drm_side) {   // the side stream's next launch may overwrite the slot this step read
+        const int rc = side_mark(c);
+        if (rc) return rc;
     }
     if (c.p32_n > 0) {
         k_point32<<<nblocks((long long)c.p32_n * m.R, 128), 128, 0, c.stream>>>(m, c.p32_node, c.p32_w, c.p32_n, uhn,

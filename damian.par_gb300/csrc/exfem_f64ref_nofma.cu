@@ -121,6 +121,27 @@ __global__ void k_drm_ref(DevModel m, int ipb) {
     drm_ref_items(m, ipb, blockIdx.x, *(volatile int *)m.d_step + 1);
 }
 
+// The DRM forces of the step after the last one computed, on the context's
+// second stream (the same items as in k_hang_ref, so the same bits): the step
+// comes from the launches' own counter, which only they advance (in their
+// stream's order), not from the step counter, which the main stream's
+// hanging pass advances at the same time.  Writes m.fdrm (the slot the
+// caller picked); the last block advances the counter.
+__global__ void __launch_bounds__(128) k_drm_ref_side(DevModel m, int ipb) {
+    const int step = *(volatile int *)m.d_drm_step + 1;
+    drm_ref_items(m, ipb, blockIdx.x, step);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(m.d_drm_blocks, 1u);
+        if (prev == gridDim.x - 1) {
+            *m.d_drm_step = step;
+            *m.d_drm_blocks = 0u;
+            __threadfence();
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) k_elem_ref(DevModel m, const double *__restrict__ u,
                                                   const double *__restrict__ um, double *__restrict__ ef) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -245,6 +266,9 @@ __global__ void __launch_bounds__(128) k_hang_ref(DevModel m, double *__restrict
                                                   int nb_recv, int ipb_drm) {
     int step = (mode == 1) ? 0 : *(volatile int *)m.d_step + 1;
     const size_t R = m.R;
+    // the step-0 sample computes step 1's DRM forces: the side-stream DRM
+    // launches continue from there
+    if (mode == 1 && blockIdx.x == 0 && threadIdx.x == 0) *m.d_drm_step = 1;
     if ((int)blockIdx.x >= nb_hang + nb_recv) {
         drm_ref_items(m, ipb_drm, (long long)blockIdx.x - nb_hang - nb_recv, step + 1);
     } else if ((int)blockIdx.x < nb_hang) {
@@ -322,16 +346,32 @@ inline int nblocks(long long work, int threads) { return (int)std::max<long long
 }  // namespace
 
 int f64ref_launch_drm_elem_node(Ctx &c, int par) {
-    DevModel &m = c.dm;
+    DevModel m = c.dm;
     double *u = c.u64[par], *um = c.u64[par ^ 1];
     const int T = 128;
-    // (this step's DRM forces came from the previous step's k_hang_ref, or
-    // for step 1 from the step-0 sample)
+    // This step's DRM forces came from the previous step's k_hang_ref (or for
+    // step 1 from the step-0 sample), or, with the second stream, from a
+    // k_drm_ref_side into slot `par` while the previous step ran; the next
+    // step's go into the other slot beside this step (side_drm_next).
+    if (c.drm_side) {
+        m.fdrm = c.fdrm64_slot[par];
+        DevModel md = c.dm;
+        md.fdrm = c.fdrm64_slot[par ^ 1];
+        const long long WD = (long long)md.ns * md.R;   // sixteen threads per (DRM element, rhs)
+        const int ipd = spread_per_block(WD, c.num_sms, T / 16);
+        const int rc = side_drm_next(c, par, [&](cudaStream_t st) {
+            k_drm_ref_side<<<spread_blocks(WD, ipd), T, 0, st>>>(md, ipd);
+            mark(c, "k_drm_ref_side");
+        });
+        if (rc) return rc;
+        c.launches++;
+    }
     k_elem_ref<<<nblocks((long long)m.ne * m.R, T), T, 0, c.stream>>>(m, u, um, c.ef64);
     mark(c, "k_elem_ref");
     k_node_ref<<<nblocks((long long)m.n_active * m.R, T), T, 0, c.stream>>>(m, c.ef64, um);
     mark(c, "k_node_ref");
     c.launches += 2;
+    if (c.drm_side && side_mark(c)) return EXFEM_E_CUDA;   // k_node_ref was the slot's reader
     return cudaGetLastError() == cudaSuccess ? EXFEM_OK : EXFEM_E_CUDA;
 }
 
@@ -344,7 +384,8 @@ int f64_launch_hang(Ctx &c, double *unew, int mode) {
     const long long WR = (long long)m.nrecv * m.R;   // four threads per (receiver, rhs)
     const int ipb = spread_per_block(WR, c.num_sms, T / 4);
     const int nbr = WR > 0 ? spread_blocks(WR, ipb) : 0;
-    const bool drm = c.opts.variant == EXFEM_VARIANT_REFERENCE_ORDER && m.ns > 0;
+    // (with the second stream the DRM forces of steps 2 and on come from there)
+    const bool drm = c.opts.variant == EXFEM_VARIANT_REFERENCE_ORDER && m.ns > 0 && (mode == 1 || !c.drm_side);
     const long long WD = drm ? (long long)m.ns * m.R : 0;   // sixteen threads per (DRM element, rhs)
     const int ipd = spread_per_block(WD, c.num_sms, T / 16);
     const int nbd = WD > 0 ? spread_blocks(WD, ipd) : 0;

@@ -286,6 +286,8 @@ int launch_step64(Ctx &c, int par) {
 }
 
 int launch_sample0_64(Ctx &c, int par) {
+    c.drm_wait[0] = c.drm_wait[1] = false;   // step 1's forces come from this launch, into slot 0
+    c.ev_step_valid = false;
     if (f64_launch_hang(c, c.u64[par], 1)) { c.err = cudaGetErrorString(cudaGetLastError()); return EXFEM_E_CUDA; }
     return EXFEM_OK;
 }
@@ -402,6 +404,14 @@ int alloc_fp64(Ctx &c) {
     TRY(dalloc(c, nst, &c.u64[0]));
     TRY(dalloc(c, nst, &c.u64[1]));
     TRY(dalloc(c, (size_t)P.ne * 8 * P.R, &c.ef64));
+    // the reference-order form runs the next step's DRM forces on a second
+    // stream too (its slot 0 is the DRM force array every form has)
+    c.drm_side = c.opts.variant == EXFEM_VARIANT_REFERENCE_ORDER && c.dm.ns > 0 && c.opts.drm_inline == 0;
+    if (c.drm_side) {
+        c.fdrm64_slot[0] = c.dm.fdrm;
+        TRY(dalloc(c, (size_t)c.dm.ns * 16 * P.R, &c.fdrm64_slot[1]));
+        TRY(side_create(c));
+    }
     return EXFEM_OK;
 }
 
@@ -423,6 +433,38 @@ void free_all(Ctx &c) {
     }
     c.allocs.clear();
 }
+
+}  // namespace
+
+namespace exfem {
+
+int side_create(Ctx &c) {
+    CK(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+    for (cudaEvent_t *e : {&c.ev_step, &c.ev_fork, &c.ev_drm[0], &c.ev_drm[1], &c.cev_step, &c.cev_drm[0],
+                           &c.cev_drm[1]})
+        CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    return EXFEM_OK;
+}
+
+int side_mark(Ctx &c) {
+    if (c.prof_on) return EXFEM_OK;
+    CK(cudaEventRecord(c.ev_step, c.stream));
+    c.ev_step_valid = true;
+    return EXFEM_OK;
+}
+
+int side_join(Ctx &c) {
+    for (int s = 0; s < 2; ++s)
+        if (c.drm_wait[s]) {
+            CK(cudaStreamWaitEvent(c.stream, c.ev_drm[s], 0));
+            c.drm_wait[s] = false;
+        }
+    return EXFEM_OK;
+}
+
+}  // namespace exfem
+
+namespace {
 
 int launch_step(Ctx &c, int par) {
     return c.precision == EXFEM_FP64 ? launch_step64(c, par) : f32_launch_step(c, par);
@@ -455,7 +497,7 @@ int capture_graph(Ctx &c, int g) {
         par ^= 1;
     }
     if (c.drm_side) {
-        const int rj = f32_join_side(c);
+        const int rj = side_join(c);
         if (!rc) rc = rj;
     }
     cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
@@ -480,8 +522,8 @@ int capture_graph(Ctx &c, int g) {
 int launches_per_step(const Ctx &c) {
     // the reference-order FP64 variant and the FP32 form compute the next
     // step's DRM forces inside their hanging/receiver kernel
-    if (c.precision == EXFEM_FP64)
-        return (c.dm.ns > 0 && c.opts.variant != EXFEM_VARIANT_REFERENCE_ORDER ? 1 : 0) + 3;   // (drm,) elem, node, hang
+    if (c.precision == EXFEM_FP64)   // (drm,) elem, node, hang
+        return (c.dm.ns > 0 && (c.opts.variant != EXFEM_VARIANT_REFERENCE_ORDER || c.drm_side) ? 1 : 0) + 3;
     return 2 + (c.p32_n > 0 ? 1 : 0) + (c.drm_side ? 1 : 0);   // step, (point,) hang, (side-stream DRM)
 }
 
@@ -672,6 +714,12 @@ int exfem_gpu_init_explicit(exfem_ctx *ctx, double *mfull_out) {
     c.steps_done = 0;
     int rc = c.precision == EXFEM_FP64 ? launch_sample0_64(c, 0) : f32_launch_sample0(c, 0);
     if (rc) return rc;
+    // the first side-stream DRM launch follows all of this (the counter reset,
+    // the step-0 sample that computes step 1's forces and sets that counter)
+    if (c.drm_side) {
+        CK(cudaEventRecord(c.ev_step, c.stream));
+        c.ev_step_valid = true;
+    }
     if (mfull_out) std::memcpy(mfull_out, c.plan.mfull_ref.data(), sizeof(double) * c.plan.mfull_ref.size());
     c.inited = true;
     return EXFEM_OK;
@@ -705,7 +753,7 @@ int exfem_gpu_run(exfem_ctx *ctx, int nsteps) {
             }
             while (left >= g) {
                 if (c.drm_side) {
-                    int rj = f32_join_side(c);
+                    int rj = side_join(c);
                     if (rj) return rj;
                 }
                 CK(cudaGraphLaunch(c.graph, c.stream));
@@ -727,7 +775,7 @@ int exfem_gpu_run(exfem_ctx *ctx, int nsteps) {
         c.steps_done++;
     }
     // the main stream covers the last side-stream launch (sync, query, events)
-    return c.drm_side ? f32_join_side(c) : EXFEM_OK;
+    return c.drm_side ? side_join(c) : EXFEM_OK;
 }
 
 int exfem_gpu_sync(exfem_ctx *ctx) {
@@ -956,7 +1004,7 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
     b += 3 * 4 * (nn + 1) + 16 * nh + 12 * nh;                     // link, gather and DRM pointers, links, hanging
     b += 4 * (4 * ne + 4 * nh);                                    // gather lists (own + hanging halves)
     b += ns * (16 + 8 + 32) + nr * (16 + 32 + 4 + 16) + R * 192;   // DRM lists, receivers, waves
-    b += 16 * std::max(ns, (size_t)1) * R * 8;                      // DRM forces
+    b += 2 * 16 * std::max(ns, (size_t)1) * R * 8;                  // DRM forces (two slots with the second stream)
     b += R * nsave * std::max(nr, (size_t)1) * 16 + 16;            // seismograms, counters
     if (f64) b += R * (nn * 32 + ne * 64);                          // u ping-pong, element forces
     else b += nn * 16 + 16 * std::max(nh, (size_t)1) + ne * 16 + 64 * std::max(ns, (size_t)1) * R + 96 * ns * R +

@@ -114,3 +114,26 @@ def test_post_critical_wave_is_rejected_not_fatal():
     with pytest.raises(ExfemError) as e:
         Solver(m)
     assert e.value.code == EXFEM_E_UNSUPPORTED
+
+
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_side_stream_drm_forces_match_the_inline_pass_fp64(use_graph):
+    """The reference-order FP64 form also computes the next step's DRM
+    forces on a second stream by default (exfem_opts.drm_inline = 0): the
+    same items in the same order as inside the hanging pass (drm_inline = 1),
+    so the results are bit for bit the same, with graph replays mixed with
+    single steps and without graphs; and they match the oracle."""
+    m = workloads.build("canyon", scale=0.12, steps=130, save_every=1, refine_band=20)
+    runs = []
+    for inline in (1, 0):
+        with Solver(m, drm_inline=inline, use_graph=use_graph) as s:
+            s.init_explicit()
+            for n in (1, 17, 40, 72):
+                s.run(n)
+            s.sync()
+            runs.append((s.seismograms(), [s.u(r) for r in range(s.nrhs)]))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    for r in range(m.problem.nrhs):
+        assert np.array_equal(runs[0][1][r], runs[1][1][r]), r
+    o = oracle.run(m, rhs=3, nthreads=NT)
+    assert fp64_rel(runs[1][0][3], o["seis"]).max() <= TOL
