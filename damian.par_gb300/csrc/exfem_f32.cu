@@ -338,6 +338,18 @@ __global__ void __launch_bounds__(256) k_drm32(DevModel m, int ipb) {
     }
 }
 
+// Per gather term, a copy of its element's four corners (the direct gather's
+// tcorn), built on the device from the term list and the element corners
+// rather than on the host and copied over: 16 bytes per term, 98 MB on the
+// 64-RHS valley.
+__global__ void k_term_corners(const int *__restrict__ tlist, const int *__restrict__ econn, int *__restrict__ tcorn,
+                               long long nterms) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nterms) return;
+    const int e = (__ldg(tlist + q) >> 1) >> 2;
+    reinterpret_cast<int4 *>(tcorn)[q] = __ldg(reinterpret_cast<const int4 *>(econn) + e);
+}
+
 // Free-field delays of the DRM corners, once per context (see
 // planewave32_delays): thread per (DRM element, corner, rhs).
 __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
@@ -1660,16 +1672,15 @@ int f32_alloc(Ctx &c) {
     // reads the corners from econn)
     m.tcorn = nullptr;
     if (direct && f32_term_corners(P.R)) {
-        pvec<int> tc;
-        tc.resize(4 * std::max<size_t>(P.tlist.size(), 1));
-        if (P.tlist.empty()) std::fill(tc.begin(), tc.end(), 0);
         const long long nt = (long long)P.tlist.size();
-#pragma omp parallel for schedule(static)
-        for (long long q = 0; q < nt; ++q) {
-            const int e = (P.tlist[q] >> 1) >> 2;
-            for (int v = 0; v < 4; ++v) tc[4 * q + v] = P.econn[(size_t)e * 4 + v];
+        int *tc = nullptr;
+        if ((rc = alloc32(c, 4 * (size_t)std::max<long long>(nt, 1), &tc))) return rc;
+        if (nt > 0) {
+            k_term_corners<<<nblocks(nt, 256), 256, 0, c.stream>>>(m.tlist, m.econn, tc, nt);
+            c.launches++;
+            CK(cudaGetLastError());
         }
-        if ((rc = upload32(c, tc, &m.tcorn))) return rc;
+        m.tcorn = tc;
     }
     return EXFEM_OK;
 }
