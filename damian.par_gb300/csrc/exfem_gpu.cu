@@ -667,7 +667,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     int rc;
     try {
         const int r_int = (o.precision == EXFEM_FP32_KAHAN && o.pad_rhs == 0) ? padded_rhs(prob->nrhs) : 0;
-        rc = build_plan(*mesh, *prob, o.reorder != 0, c->plan, c->err, r_int);
+        rc = build_plan(*mesh, *prob, o.reorder != 0, c->plan, c->err, r_int, o.precision == EXFEM_FP64);
     } catch (const std::bad_alloc &) {
         rc = EXFEM_E_NOMEM;
         c->err = "host allocation failed while preparing the model";

@@ -15,13 +15,14 @@ const double F_WANGZERO = (double)0.0001f;   // pwaves.f90:8 (single literal in 
 inline bool realunder(double a, double b) { return (a - b) < -U_TOL; }
 inline bool realover(double a, double b) { return (a - b) > U_TOL; }
 
-uint64_t spread21(uint64_t v) {
+// 21 bits to the even bit positions 0, 2, ..., 40 (a 2-D Morton interleave).
+uint64_t spread2(uint64_t v) {
     v &= 0x1fffff;
-    v = (v | v << 32) & 0x1f00000000ffffULL;
-    v = (v | v << 16) & 0x1f0000ff0000ffULL;
-    v = (v | v << 8) & 0x100f00f00f00f00fULL;
-    v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
-    v = (v | v << 2) & 0x1249249249249249ULL;
+    v = (v | v << 16) & 0x001f0000ffffULL;
+    v = (v | v << 8) & 0x001f00ff00ffULL;
+    v = (v | v << 4) & 0x010f0f0f0f0fULL;
+    v = (v | v << 2) & 0x013333333333ULL;
+    v = (v | v << 1) & 0x015555555555ULL;
     return v;
 }
 
@@ -40,7 +41,8 @@ struct Morton {
     }
     uint64_t key(double x, double y) const {
         uint64_t ix = (uint64_t)std::llround((x - x0) * sx), iy = (uint64_t)std::llround((y - y0) * sy);
-        return spread21(ix) | (spread21(iy) << 1);
+        // y bit b above x bit b above y bit b - 1: keys below 2^42
+        return spread2(ix) | (spread2(iy) << 1);
     }
 };
 }  // namespace
@@ -192,8 +194,62 @@ struct KeyId {
     uint64_t key;
     int id;
 };
-static void radix_order(const uint64_t *key, int *idx, long long n) {
+// The same order from 8-byte records: a key below 2^42 and an id below 2^22
+// packed as key << 22 | id, sorted on the key bits only.  The ids start
+// increasing (the callers' initial orders), so the stable passes leave equal
+// keys in id order, as the 16-byte form does; half the bytes per pass.
+static void radix_order_packed(const uint64_t *key, int *idx, long long n) {
+    constexpr int BITS = 11;
+    constexpr int NB = 1 << BITS;
+    constexpr int IDB = 22;
+    const int nch = (int)std::min<long long>(64, std::max<long long>(1, n / 16384));
+    const long long chunk = (n + nch - 1) / nch;
+    pvec<uint64_t> a, b;
+    a.resize(n);
+    b.resize(n);
+    uint64_t any = 0, all = ~0ull;
+#pragma omp parallel for schedule(static) reduction(| : any) reduction(& : all)
+    for (long long i = 0; i < n; ++i) {
+        a[i] = (key[idx[i]] << IDB) | (uint64_t)idx[i];
+        any |= a[i];
+        all &= a[i];
+    }
+    std::vector<long long> off((size_t)NB * nch);
+    for (int sh = IDB; sh < 64; sh += BITS) {
+        if ((((any ^ all) >> sh) & (NB - 1)) == 0) continue;
+#pragma omp parallel for schedule(static, 1)
+        for (int t = 0; t < nch; ++t) {
+            long long h[NB] = {0};
+            const long long lo = t * chunk, hi = std::min(n, lo + chunk);
+            for (long long i = lo; i < hi; ++i) h[(a[i] >> sh) & (NB - 1)]++;
+            for (int d = 0; d < NB; ++d) off[(size_t)d * nch + t] = h[d];
+        }
+        long long run = 0;
+        for (size_t i = 0; i < off.size(); ++i) {
+            const long long c = off[i];
+            off[i] = run;
+            run += c;
+        }
+#pragma omp parallel for schedule(static, 1)
+        for (int t = 0; t < nch; ++t) {
+            long long h[NB];
+            for (int d = 0; d < NB; ++d) h[d] = off[(size_t)d * nch + t];
+            const long long lo = t * chunk, hi = std::min(n, lo + chunk);
+            for (long long i = lo; i < hi; ++i) b[h[(a[i] >> sh) & (NB - 1)]++] = a[i];
+        }
+        a.swap(b);
+    }
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; ++i) idx[i] = (int)(a[i] & ((1ull << IDB) - 1));
+}
+
+static void radix_order(const uint64_t *key, int *idx, long long n, long long id_bound) {
     if (n < 2) return;
+    // Morton keys are 42 bits: ids below 2^22 pack beside them
+    if (id_bound <= (1LL << 22)) {
+        radix_order_packed(key, idx, n);
+        return;
+    }
     constexpr int BITS = 11;
     constexpr int NB = 1 << BITS;
     const int nch = (int)std::min<long long>(64, std::max<long long>(1, n / 16384));   // chunks per pass
@@ -238,7 +294,7 @@ static void radix_order(const uint64_t *key, int *idx, long long n) {
 }
 
 int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &P, std::string &err,
-               int r_internal) {
+               int r_internal, bool fp64_operator) {
     const int nn = mesh.nnodes, ne = mesh.nelems;
     if (nn <= 0 || ne <= 0 || !mesh.eptr || !mesh.eind || !mesh.ediv || !mesh.nodes || !mesh.ematprop) {
         err = "mesh arrays missing or empty";
@@ -369,7 +425,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         keys.resize(nn);
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < nn; ++i) keys[i] = mort.key(xs[i], ys[i]);
-        radix_order(keys.data(), order.data(), (long long)order.size());
+        radix_order(keys.data(), order.data(), (long long)order.size(), nn);
     }
     order.resize(nn);
     for (int i = 0; i < prob.nhanging; ++i) order[(size_t)P.n_active + i] = prob.hanging[3 * i] - 1;
@@ -392,7 +448,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
             double cy = 0.25 * (ys[c[0]] + ys[c[1]] + ys[c[2]] + ys[c[3]]);
             ek[e] = mort.key(cx, cy);
         }
-        radix_order(ek.data(), eorder.data(), ne);
+        radix_order(ek.data(), eorder.data(), ne, ne);
     }
     pvec<int> &elem_of_ref = P.elem_of_ref;   // kept for point sampling
     elem_of_ref.resize(ne);
@@ -401,11 +457,17 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
 
     // ---- per-element data (internal order); dashpot slots numbered in that order
     P.econn.resize((size_t)ne * 4);
-    P.ecoef.resize((size_t)ne * 4);
     P.ecoef32.resize((size_t)ne * 4);
     P.emass.resize(ne);
-    P.emulam.resize((size_t)ne * 2);
-    P.ekv.resize((size_t)ne * 6);
+    if (fp64_operator) {
+        P.ecoef.resize((size_t)ne * 4);
+        P.emulam.resize((size_t)ne * 2);
+        P.ekv.resize((size_t)ne * 6);
+    } else {
+        P.ecoef.clear();
+        P.emulam.clear();
+        P.ekv.clear();
+    }
     P.edampv.clear();
     pvec<double> eh;
     eh.resize(ne);
@@ -423,14 +485,15 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         damped[ie] = 0;
         if (!(h > 0) || !(rho > 0)) { bad_elem = std::min(bad_elem, e); continue; }
         eh[ie] = h;
-        P.emulam[(size_t)ie * 2] = mu;
-        P.emulam[(size_t)ie * 2 + 1] = lam;
-        calck_values(mu, lam, &P.ekv[(size_t)ie * 6]);
-        P.ecoef[(size_t)ie * 4 + 0] = (lam + 2.0 * mu) / 4.0;
-        P.ecoef[(size_t)ie * 4 + 1] = lam / 4.0;
-        P.ecoef[(size_t)ie * 4 + 2] = mu / 4.0;
-        P.ecoef[(size_t)ie * 4 + 3] = (lam + 3.0 * mu) / 12.0;
-        for (int k = 0; k < 4; ++k) P.ecoef32[(size_t)ie * 4 + k] = (float)P.ecoef[(size_t)ie * 4 + k];
+        // the closed form's coefficients, in FP64, and rounded once for FP32
+        const double co[4] = {(lam + 2.0 * mu) / 4.0, lam / 4.0, mu / 4.0, (lam + 3.0 * mu) / 12.0};
+        for (int k = 0; k < 4; ++k) P.ecoef32[(size_t)ie * 4 + k] = (float)co[k];
+        if (fp64_operator) {
+            P.emulam[(size_t)ie * 2] = mu;
+            P.emulam[(size_t)ie * 2 + 1] = lam;
+            calck_values(mu, lam, &P.ekv[(size_t)ie * 6]);
+            for (int k = 0; k < 4; ++k) P.ecoef[(size_t)ie * 4 + k] = co[k];
+        }
         double scl = h / 2.0;
         P.emass[ie] = (scl * scl) * rho;   // calcm (formulation.f90:250-254)
         for (int k = 0; k < 4; ++k) {

@@ -193,8 +193,11 @@ bool build_pipe_pack(const Plan &P, const Tiles &T, int max_runs, PipePack &out,
 // Build the plan.  Returns EXFEM_OK or an EXFEM_E_* code with err filled.
 // r_internal > prob.nrhs pads the right-hand sides with zero-amplitude waves
 // (see padded_rhs); the plan's arrays then carry r_internal of them.
+// fp64_operator false (an FP32 context) leaves out the arrays only the FP64
+// kernels read: the per-element calck values, FP64 closed-form coefficients
+// and (mu, lambda) pairs (ekv, ecoef, emulam stay empty).
 int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, Plan &plan, std::string &err,
-               int r_internal = 0);
+               int r_internal = 0, bool fp64_operator = true);
 
 // Internal right-hand-side count of the FP32 form for R of the caller's.  A
 // node's row holds R floats; when R is odd its rows are not 8-byte aligned,
