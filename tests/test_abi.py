@@ -56,6 +56,11 @@ def test_argument_errors_need_no_device():
     bad = default_opts(index_bits=32)   # 0 (automatic) or 64
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
     assert b"index_bits" in L.exfem_gpu_last_error(None)
+    assert default_opts().drm_inline == 0 and default_opts().tune == 0
+    for field, bad_value in (("drm_inline", 2), ("tune", 2)):
+        bad = default_opts(**{field: bad_value})
+        assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
+        assert field.encode() in L.exfem_gpu_last_error(None)
     assert default_opts().wait_cycles == 0       # the library's default bound
     bad = default_opts(wait_cycles=-1)
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
@@ -77,3 +82,19 @@ def test_estimate_counts_rhs_padding():
     assert estimate_bytes(m, precision=0) == estimate_bytes(m, precision=0, pad_rhs=1)
     even = workloads.build("canyon", scale=0.1, steps=10, waves=waves[:12])
     assert estimate_bytes(even, precision=1) == estimate_bytes(even, precision=1, pad_rhs=1)
+
+
+def test_server_defaults_keep_the_drm_pass_inline():
+    """The server's default solver options run every request's DRM forces in
+    its hanging/receiver pass (drm_inline = 1): with many requests stepping at
+    once, a second stream per request measured slower.  A context made
+    directly defaults to the second stream (drm_inline = 0)."""
+    import ctypes as C
+
+    from exfem.abi import SrvOpts
+    from exfem.gpu import default_opts
+    from exfem.serve import srv_lib
+    o = SrvOpts()
+    srv_lib().exfem_srv_default_opts(C.byref(o))
+    assert o.solver.drm_inline == 1 and o.solver.precision == 1
+    assert default_opts().drm_inline == 0

@@ -369,6 +369,21 @@ def test_bounded_wait_runs_out_and_reports_a_status():
     a, ua = run32(m, variant=0)
     b, ub = run32(m, variant=2)
     assert np.array_equal(a, b)
+    # the tensor-core step's wait for its MMAs is bounded the same way: it
+    # gives up, flags, still waits (with the default bound) for the MMAs
+    # before it frees their TMEM, and returns
+    m16 = workloads.build("canyon", scale=0.15, steps=40, save_every=2, waves=EIGHT_WAVES + EIGHT_WAVES)
+    with Solver(m16, precision=EXFEM_FP32_KAHAN, variant=3, wait_cycles=1) as s:
+        s.init_explicit()
+        names = s.kernel_times(2)
+        assert "k_mma32" in names, names
+        with pytest.raises(ExfemError) as e:
+            s.sync()
+        assert e.value.code == EXFEM_E_TIMEOUT
+    c, _ = run32(m16, variant=3)
+    d, _ = run32(m16, variant=0)
+    for r in range(16):
+        assert per_receiver_rel(c[r], d[r]).max() <= TOL, r
 
 
 @pytest.mark.parametrize("nrhs_waves", [1, 8, 12])
