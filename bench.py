@@ -493,7 +493,7 @@ def run_ours(args, ws, rank, local, dist, torch):
     for _ in range(3):   # three requests; the median is reported
         t0 = time.perf_counter()
         se = Solver(me, precision=form, device=local, **tuned)
-        se.init_explicit()
+        se.init_explicit(want_mfull=False)   # the request's result is its seismograms
         se.run(e2e_steps)
         seis = se.seismograms()
         h2d, d2h = se.copy_bytes()

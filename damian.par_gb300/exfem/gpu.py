@@ -66,7 +66,12 @@ class Solver:
         if rc != 0:
             raise ExfemError(rc, self.lib.exfem_gpu_last_error(self.h).decode())
 
-    def init_explicit(self):
+    def init_explicit(self, want_mfull=True):
+        """init_explicit; returns m_full (mass.bin's content), or None with
+        want_mfull False (no host copy of it)."""
+        if not want_mfull:
+            self._check(self.lib.exfem_gpu_init_explicit(self.h, None))
+            return None
         mfull = np.zeros(2 * self.model.nnodes)
         self._check(self.lib.exfem_gpu_init_explicit(self.h, _dp(mfull)))
         return mfull
