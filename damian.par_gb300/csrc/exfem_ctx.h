@@ -56,6 +56,12 @@ struct DevModel {
     const float *hcoef4;           // per hanging entry: -2 a2 C (x, y), a1 M + a2 C (x, y)
     float *fdrm32;                 // ns * 8 * R DRM forces (FP64 math, stored FP32)
     const int *tcorn;              // 4 per gather term: the corners of its element
+    // the direct gather's fixed-size node records (build_node_slots; null in
+    // the list form): 4 term entries and 1/m_full (negative: marked) per
+    // active node, and with term corners 4 x 4 corners per active node
+    const int *tslot4;
+    const float *ninvm;
+    const int *tcorn4;
     const double *drm_delay;       // ((s*4 + corner)*3 + term)*R + r: the DRM corners' free-field delays
     // point source (EXFEM_POINT_*; 0 = none)
     int point_kind, npoint;
@@ -168,6 +174,20 @@ inline int spread_blocks(long long items, int per_block) {
 // measured 12% faster with one RHS and, with a node's rows paired, 12% at
 // four (0.55M-element valley); the copy is 1-2% faster from six.
 constexpr bool f32_term_corners(int R) { return R > 4; }
+// The same choice for the fixed-size node records (4 x 16 B per node in
+// tcorn4).  Measured with the records on the 1.5M-element valley at one RHS
+// and on 0.52M- and 0.86M-element requests at two: copies at every R were
+// 10-27% slower than econn up to four RHS.
+constexpr bool f32_slot_corners(int R) { return R > 4; }
+
+// FP32 direct gather: active nodes from which the fixed-size node records
+// (build_node_slots) replace the list form.  A marked node's path is longer
+// with them (its slot terms, then its lists), and a mesh this small runs in
+// one partial wave of blocks, so its step lasts as long as its slowest warp:
+// measured 5-8% slower with the records on 34K- and 36K-element requests,
+// the same at 55K-74K, and 3-11% faster from 0.13M elements (the 1.5M-element
+// valley: 7% at one RHS, 4% at 64).
+constexpr int kSlotMinNodes = 50000;
 
 // FP32 direct gather with several threads per node: whether the state is laid
 // out in groups of one thread's right-hand sides (row_off), so that a thread's

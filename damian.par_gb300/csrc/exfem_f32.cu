@@ -350,6 +350,18 @@ __global__ void k_term_corners(const int *__restrict__ tlist, const int *__restr
     reinterpret_cast<int4 *>(tcorn)[q] = __ldg(reinterpret_cast<const int4 *>(econn) + e);
 }
 
+// The slot form's corner copies: for slot j of active node n (an entry, or
+// -1), the four corners of its element at tcorn4[4 * (4n + j)], from the slot
+// records and the element corners (an empty slot gets -1s, never read).
+__global__ void k_slot_corners(const int *__restrict__ slot4, const int *__restrict__ econn, int *__restrict__ tcorn4,
+                               long long nslots) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nslots) return;
+    const int ent = __ldg(slot4 + q);
+    reinterpret_cast<int4 *>(tcorn4)[q] =
+        ent < 0 ? make_int4(-1, -1, -1, -1) : __ldg(reinterpret_cast<const int4 *>(econn) + ((ent >> 1) >> 2));
+}
+
 // Free-field delays of the DRM corners, once per context (see
 // planewave32_delays): thread per (DRM element, corner, rhs).
 __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
@@ -368,13 +380,18 @@ __global__ void k_drm_delays32(DevModel m, double *__restrict__ out) {
 // the dashpot term, the hanging nodes it anchors, and the Kahan-compensated
 // increment update of D and u (shared by the direct gather and the
 // tensor-core step).
-template <int RPT, bool PAIR, typename I>
+// SLOT: the node's record came from the fixed-size slots (build_node_slots):
+// an unmarked node (invm > 0) has 1/m_full = invm in x and y, no dashpot and
+// anchors no hanging node, so it reads neither ncoef4 nor the anchor list.
+template <int RPT, bool PAIR, typename I, bool SLOT = false>
 __device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R, I roff, float (&ax)[RPT],
                                             float (&ay)[RPT], const float *__restrict__ uh,
                                             float *__restrict__ uhn, unsigned short *__restrict__ uc,
-                                            float *__restrict__ dh, unsigned short *__restrict__ dc) {
+                                            float *__restrict__ dh, unsigned short *__restrict__ dc,
+                                            float invm = -1.f) {
     // dashpot term -2 a2 C D (zero away from the absorbing boundary)
-    const float4 nc = __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
+    const bool plain = SLOT && invm > 0.f;
+    const float4 nc = plain ? make_float4(invm, invm, 0.f, 0.f) : __ldg(reinterpret_cast<const float4 *>(m.ncoef4) + n);
     float dx[RPT], dy[RPT];
     XY<RPT, PAIR>::load_cg(dh + bn, R, dx, dy);
     if (nc.z != 0.f || nc.w != 0.f) {
@@ -387,7 +404,7 @@ __device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R,
     //   1/2 [ -2 a2 C_h D_h + D_h,mass ((u_h - u_n) + (D_h - D_n)) ]
     // (u_h, D_h from the hanging node's rows, which change only in k_hang32;
     // the other anchor's row is rewritten in place during this kernel)
-    for (int q = m.lptr[n]; q < m.lptr[n + 1]; ++q) {
+    for (int q = plain ? 0 : m.lptr[n]; q < (plain ? 0 : m.lptr[n + 1]); ++q) {
         int h = __ldg(m.llist + 2 * q);
         float4 hc = __ldg(reinterpret_cast<const float4 *>(m.hcoef4) + (h - m.n_active));
         I bh = ((I)h * 2) * R + roff;
@@ -425,6 +442,32 @@ __device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R,
     XY<RPT, PAIR>::store(uhn + bn, R, ox, oy);
 }
 
+// One element term of a node's gather: -K_e u_e at the node's corner c of
+// element e (weight 1/2 for a hanging node's term carried by its anchor),
+// ent = ((e*4 + c) << 1) | half, cn = the element's corners.
+template <int RPT, bool PAIR, typename I>
+__device__ __forceinline__ void gather_term(const DevModel &m, int ent, int4 cn, I R, I roff,
+                                            const float *__restrict__ uh, float (&ax)[RPT], float (&ay)[RPT]) {
+    float w = (ent & 1) ? 0.5f : 1.0f;
+    int ec = ent >> 1;
+    int e = ec >> 2, c = ec & 3;
+    float4 k = __ldg(reinterpret_cast<const float4 *>(m.ecoef32) + e);
+    const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
+    float ux[4][RPT], uy[4][RPT];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        I b = ((I)cc[v] * 2) * R + roff;
+        XY<RPT, PAIR>::load(uh + b, R, ux[v], uy[v]);
+    }
+    const Q4Fold<float> f = q4_fold<float>(k.x, k.y, k.z, k.w, c, w);
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
+        float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
+        q4_corner_acc<float>(f, vx, vy, ax[j], ay[j]);
+    }
+}
+
 // The fused step for one non-hanging node and RPT right-hand sides.  The
 // corners of each term's element come from the per-term copy m.tcorn, loaded
 // beside the term itself (not from econn after it), so the gather chain is
@@ -439,7 +482,13 @@ __device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R,
 // PAIR: the state is grouped by RPT (m.lg == RPT, row_off; with RPT == R
 // that is the plain layout), so the thread's x and y values of a node are
 // adjacent and load and store as one vector (XY).
-template <int RPT, bool I32, bool TC, bool PAIR>
+// SLOT: the node's first four terms and its 1/m_full come from its
+// fixed-size slot record (m.tslot4, m.ninvm; build_node_slots), loaded with
+// nothing before them, and with TC the corners of those terms from m.tcorn4
+// (4 per node); only a marked node (invm < 0) reads its DRM list, its terms
+// past the fourth (corners from econn), ncoef4 and its anchor list.  The terms
+// are added in the same order as the list form, so results are bit-identical.
+template <int RPT, bool I32, bool TC, bool PAIR, bool SLOT>
 __device__ __forceinline__ void step32_tile(const DevModel &m, unsigned tile, const float *__restrict__ uh,
                                             float *__restrict__ uhn, unsigned short *__restrict__ uc,
                                             float *__restrict__ dh, unsigned short *__restrict__ dc) {
@@ -501,62 +550,71 @@ __device__ __forceinline__ void step32_tile(const DevModel &m, unsigned tile, co
     float ax[RPT], ay[RPT];
 #pragma unroll
     for (int j = 0; j < RPT; ++j) { ax[j] = 0.f; ay[j] = 0.f; }
+    int4 s4 = make_int4(-1, -1, -1, -1);
+    float invm = -1.f;
+    if constexpr (SLOT) {
+        s4 = __ldg(reinterpret_cast<const int4 *>(m.tslot4) + n);
+        invm = __ldg(m.ninvm + n);
+    }
     // DRM terms (hanging corners at half weight in their anchors)
-    for (int q = m.dptr[n]; q < m.dptr[n + 1]; ++q) {
-        int ent = __ldg(m.dlist + q);
-        float w = (ent & 1) ? 0.5f : 1.0f;
-        int sc = ent >> 1;
-        I b = ((I)(sc >> 2) * 8 + 2 * (sc & 3)) * R + roff;
-        float fx[RPT], fy[RPT];
-        XY<RPT, PAIR>::load_cg(m.fdrm32 + b, R, fx, fy);
+    if (!SLOT || invm < 0.f) {
+        for (int q = m.dptr[n]; q < m.dptr[n + 1]; ++q) {
+            int ent = __ldg(m.dlist + q);
+            float w = (ent & 1) ? 0.5f : 1.0f;
+            int sc = ent >> 1;
+            I b = ((I)(sc >> 2) * 8 + 2 * (sc & 3)) * R + roff;
+            float fx[RPT], fy[RPT];
+            XY<RPT, PAIR>::load_cg(m.fdrm32 + b, R, fx, fy);
 #pragma unroll
-        for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
+            for (int j = 0; j < RPT; ++j) { ax[j] += w * fx[j]; ay[j] += w * fy[j]; }
+        }
     }
     // element terms: -K_e u_e at this node's corner (and its hanging nodes' at 1/2)
-    const float4 *coef4 = reinterpret_cast<const float4 *>(m.ecoef32);
-    for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
-        int ent = __ldg(m.tlist + q);
-        int4 cn;
-        if constexpr (TC) cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn) + q);
-        float w = (ent & 1) ? 0.5f : 1.0f;
-        int ec = ent >> 1;
-        int e = ec >> 2, c = ec & 3;
-        if constexpr (!TC) cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + e);
-        float4 k = __ldg(coef4 + e);
-        const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
-        float ux[4][RPT], uy[4][RPT];
+    if constexpr (SLOT) {
+        const int sl[4] = {s4.x, s4.y, s4.z, s4.w};
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            I b = ((I)cc[v] * 2) * R + roff;
-            XY<RPT, PAIR>::load(uh + b, R, ux[v], uy[v]);
+        for (int j = 0; j < 4; ++j) {
+            if (sl[j] < 0) continue;   // only trailing slots are empty
+            int4 cn;
+            if constexpr (TC) cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn4) + ((I)n * 4 + j));
+            else cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + ((sl[j] >> 1) >> 2));
+            gather_term<RPT, PAIR, I>(m, sl[j], cn, R, roff, uh, ax, ay);
         }
-        const Q4Fold<float> f = q4_fold<float>(k.x, k.y, k.z, k.w, c, w);
-#pragma unroll
-        for (int j = 0; j < RPT; ++j) {
-            float vx[4] = {ux[0][j], ux[1][j], ux[2][j], ux[3][j]};
-            float vy[4] = {uy[0][j], uy[1][j], uy[2][j], uy[3][j]};
-            q4_corner_acc<float>(f, vx, vy, ax[j], ay[j]);
+        if (invm < 0.f) {
+            for (int q = m.tptr[n] + 4; q < m.tptr[n + 1]; ++q) {
+                const int ent = __ldg(m.tlist + q);
+                gather_term<RPT, PAIR, I>(m, ent, __ldg(reinterpret_cast<const int4 *>(m.econn) + ((ent >> 1) >> 2)),
+                                          R, roff, uh, ax, ay);
+            }
+        }
+    } else {
+        for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
+            int ent = __ldg(m.tlist + q);
+            int4 cn;
+            if constexpr (TC) cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn) + q);
+            else cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + ((ent >> 1) >> 2));
+            gather_term<RPT, PAIR, I>(m, ent, cn, R, roff, uh, ax, ay);
         }
     }
-    node_update<RPT, PAIR, I>(m, n, bn, R, roff, ax, ay, uh, uhn, uc, dh, dc);
+    node_update<RPT, PAIR, I, SLOT>(m, n, bn, R, roff, ax, ay, uh, uhn, uc, dh, dc, invm);
 }
 
-template <int RPT, bool I32, bool TC = true, bool PAIR = false>
+template <int RPT, bool I32, bool TC = true, bool PAIR = false, bool SLOT = false>
 __global__ void __launch_bounds__(512) k_step32(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                 unsigned short *__restrict__ uc, float *__restrict__ dh,
                                                 unsigned short *__restrict__ dc) {
-    step32_tile<RPT, I32, TC, PAIR>(m, blockIdx.x, uh, uhn, uc, dh, dc);
+    step32_tile<RPT, I32, TC, PAIR, SLOT>(m, blockIdx.x, uh, uhn, uc, dh, dc);
 }
 
 // The same step as a persistent kernel (variant 4): a grid of as many blocks
 // as fit on the device at once, each striding over the block-sized tiles of
 // (node, RHS group) threads that k_step32 gives one block each.
-template <int RPT, bool I32, bool TC = true, bool PAIR = false>
+template <int RPT, bool I32, bool TC = true, bool PAIR = false, bool SLOT = false>
 __global__ void __launch_bounds__(512) k_step32p(DevModel m, const float *__restrict__ uh, float *__restrict__ uhn,
                                                  unsigned short *__restrict__ uc, float *__restrict__ dh,
                                                  unsigned short *__restrict__ dc, unsigned ntiles) {
     for (unsigned tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-        step32_tile<RPT, I32, TC, PAIR>(m, tile, uh, uhn, uc, dh, dc);
+        step32_tile<RPT, I32, TC, PAIR, SLOT>(m, tile, uh, uhn, uc, dh, dc);
 }
 
 // Tiled variant of k_step32: a block owns `tn` consecutive active nodes (a
@@ -1617,7 +1675,7 @@ int f32_alloc(Ctx &c) {
     // (measured on 0.1M- and 0.55M-element valleys: 1-3% faster than 256 on
     // the larger mesh, within 2% either way on the smaller)
     if (c.opts.block_threads <= 0)
-        c.block_threads = (P.R >= 4 && (c.opts.variant == 0 || c.opts.variant == 4)) ? 128 : 256;
+        c.block_threads = (P.R >= 4 && (c.opts.variant == 0 || c.opts.variant == 4 || c.opts.variant == 5)) ? 128 : 256;
     // shared-memory tiles (variant 1; variant 0, the default, is the direct gather)
     c.use_tiles = false;
     if (c.opts.variant == 1) {
@@ -1668,10 +1726,33 @@ int f32_alloc(Ctx &c) {
     // the thread's RHS (the tiled variants read the plain layout)
     const bool direct = !c.use_tiles && !c.use_pipe && !c.use_mma;
     m.lg = (direct && c.rhs_per_thread < P.R && f32_interleave(P.R)) ? c.rhs_per_thread : P.R;
-    // the direct gather's per-term corner copies (with few RHS k_step32
-    // reads the corners from econn)
+    // the direct gather's fixed-size node records from kSlotMinNodes active
+    // nodes (variant 5: the list form always)
+    m.tslot4 = nullptr;
+    m.ninvm = nullptr;
+    m.tcorn4 = nullptr;
+    if (direct && c.opts.variant != 5 && P.n_active >= kSlotMinNodes) {
+        NodeSlots S;
+        std::string why;
+        if (build_node_slots(P, nc, S, why)) {
+            if ((rc = upload32(c, S.slot4, &m.tslot4)) || (rc = upload32(c, S.invm, &m.ninvm))) return rc;
+            if (f32_slot_corners(P.R)) {
+                const long long ns4 = 4 * (long long)P.n_active;
+                int *tc = nullptr;
+                if ((rc = alloc32(c, 4 * (size_t)std::max<long long>(ns4, 1), &tc))) return rc;
+                if (ns4 > 0) {
+                    k_slot_corners<<<nblocks(ns4, 256), 256, 0, c.stream>>>(m.tslot4, m.econn, tc, ns4);
+                    c.launches++;
+                    CK(cudaGetLastError());
+                }
+                m.tcorn4 = tc;
+            }
+        }
+    }
+    // the direct gather's per-term corner copies in the list form (with few
+    // RHS k_step32 reads the corners from econn)
     m.tcorn = nullptr;
-    if (direct && f32_term_corners(P.R)) {
+    if (direct && !m.tslot4 && f32_term_corners(P.R)) {
         const long long nt = (long long)P.tlist.size();
         int *tc = nullptr;
         if ((rc = alloc32(c, 4 * (size_t)std::max<long long>(nt, 1), &tc))) return rc;
@@ -1768,24 +1849,65 @@ int f32_init(Ctx &c) {
 }
 
 // k_step32 with 32- or 64-bit indices as the context allows.
-template <int RPT, bool TC, bool PAIR>
+template <int RPT, bool TC, bool PAIR, bool SLOT>
 static void step32(Ctx &c, const DevModel &m, int nb, int T, const float *uh, float *uhn) {
     if (c.opts.variant == 4) {   // persistent: the blocks that fit at once stride over the tiles
         if (c.persist_grid <= 0) {
             int per = 0;
-            if (c.idx32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step32p<RPT, true, TC, PAIR>, T, 0);
-            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step32p<RPT, false, TC, PAIR>, T, 0);
+            if (c.idx32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step32p<RPT, true, TC, PAIR, SLOT>, T, 0);
+            else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step32p<RPT, false, TC, PAIR, SLOT>, T, 0);
             c.persist_grid = std::max(1, per) * c.num_sms;
         }
         const int g = std::min(nb, c.persist_grid);
         if (c.idx32)
-            k_step32p<RPT, true, TC, PAIR><<<g, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, (unsigned)nb);
+            k_step32p<RPT, true, TC, PAIR, SLOT><<<g, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, (unsigned)nb);
         else
-            k_step32p<RPT, false, TC, PAIR><<<g, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, (unsigned)nb);
+            k_step32p<RPT, false, TC, PAIR, SLOT><<<g, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp, (unsigned)nb);
         return;
     }
-    if (c.idx32) k_step32<RPT, true, TC, PAIR><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
-    else k_step32<RPT, false, TC, PAIR><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+    if (c.idx32) k_step32<RPT, true, TC, PAIR, SLOT><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+    else k_step32<RPT, false, TC, PAIR, SLOT><<<nb, T, 0, c.stream>>>(m, uh, uhn, c.ucomp, c.udel[0], c.dcomp);
+}
+
+// The direct gather's kernel for the context's shape: RHS per thread, term
+// corners (copies or econn), paired rows, slot records or lists.
+template <bool SLOT>
+static int step32_pick(Ctx &c, const DevModel &m, int nb, int T, const float *uh, float *uhn) {
+    const int rpt = c.rhs_per_thread;
+    // rows paired when the state is grouped by the thread's RHS (or a thread
+    // holds the whole node)
+    const bool pair = m.lg == rpt;
+    const bool tc = SLOT ? m.tcorn4 != nullptr : m.tcorn != nullptr;
+    if (!tc) {   // few RHS (f32_term_corners): corners from econn
+        // below 64 RHS the direct gather's state is always grouped by the
+        // thread's RHS (f32_alloc), so these rows are always paired
+        static_assert(f32_term_corners(5) && f32_interleave(4), "econn corners only with grouped rows");
+        if (!pair) {
+            c.err = "internal: few-RHS step on the plain layout";
+            return EXFEM_E_STATE;
+        }
+        switch (rpt) {
+            case 4: step32<4, false, true, SLOT>(c, m, nb, T, uh, uhn); break;
+            case 2: step32<2, false, true, SLOT>(c, m, nb, T, uh, uhn); break;
+            default: step32<1, false, true, SLOT>(c, m, nb, T, uh, uhn); break;
+        }
+        return EXFEM_OK;
+    }
+    switch (rpt) {
+        case 4:
+            if (pair) step32<4, true, true, SLOT>(c, m, nb, T, uh, uhn);
+            else step32<4, true, false, SLOT>(c, m, nb, T, uh, uhn);
+            break;
+        case 2:
+            if (pair) step32<2, true, true, SLOT>(c, m, nb, T, uh, uhn);
+            else step32<2, true, false, SLOT>(c, m, nb, T, uh, uhn);
+            break;
+        default:
+            if (pair) step32<1, true, true, SLOT>(c, m, nb, T, uh, uhn);
+            else step32<1, true, false, SLOT>(c, m, nb, T, uh, uhn);
+            break;
+    }
+    return EXFEM_OK;
 }
 
 int f32_launch_step(Ctx &c, int par) {
@@ -1848,38 +1970,8 @@ int f32_launch_step(Ctx &c, int par) {
         mark(c, "k_tile32");
     } else {
     const int nb = nblocks(work, T);
-    // rows paired when the state is grouped by the thread's RHS (or a thread
-    // holds the whole node)
-    const bool pair = m.lg == rpt;
-    if (!m.tcorn) {   // few RHS (f32_term_corners): corners from econn
-        // below 64 RHS the direct gather's state is always grouped by the
-        // thread's RHS (f32_alloc), so these rows are always paired
-        static_assert(f32_term_corners(5) && f32_interleave(4), "econn corners only with grouped rows");
-        if (!pair) {
-            c.err = "internal: few-RHS step on the plain layout";
-            return EXFEM_E_STATE;
-        }
-        switch (rpt) {
-            case 4: step32<4, false, true>(c, m, nb, T, uh, uhn); break;
-            case 2: step32<2, false, true>(c, m, nb, T, uh, uhn); break;
-            default: step32<1, false, true>(c, m, nb, T, uh, uhn); break;
-        }
-    } else {
-        switch (rpt) {
-            case 4:
-                if (pair) step32<4, true, true>(c, m, nb, T, uh, uhn);
-                else step32<4, true, false>(c, m, nb, T, uh, uhn);
-                break;
-            case 2:
-                if (pair) step32<2, true, true>(c, m, nb, T, uh, uhn);
-                else step32<2, true, false>(c, m, nb, T, uh, uhn);
-                break;
-            default:
-                if (pair) step32<1, true, true>(c, m, nb, T, uh, uhn);
-                else step32<1, true, false>(c, m, nb, T, uh, uhn);
-                break;
-        }
-    }
+    const int rc = m.tslot4 ? step32_pick<true>(c, m, nb, T, uh, uhn) : step32_pick<false>(c, m, nb, T, uh, uhn);
+    if (rc) return rc;
     c.launches++;
     mark(c, c.opts.variant == 4 ? "k_step32p" : "k_step32");
     }

@@ -640,7 +640,7 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     if (opts) o = *opts;
     else exfem_gpu_default_opts(&o);
     if (o.precision != EXFEM_FP64 && o.precision != EXFEM_FP32_KAHAN) { g_create_err = "unknown precision"; return EXFEM_E_ARG; }
-    if (o.variant < 0 || o.variant > (o.precision == EXFEM_FP32_KAHAN ? 4 : 1)) {
+    if (o.variant < 0 || o.variant > (o.precision == EXFEM_FP32_KAHAN ? 5 : 1)) {
         g_create_err = "unknown kernel variant";
         return EXFEM_E_ARG;
     }

@@ -929,6 +929,27 @@ pvec<float> node_coef32(const Plan &P) {
     return nc;
 }
 
+bool build_node_slots(const Plan &P, const pvec<float> &nc, NodeSlots &out, std::string &why) {
+    out = NodeSlots();
+    if ((long long)P.ne * 8 > (1ll << 31) - 1) { why = "2^28 elements or more"; return false; }
+    out.slot4.resize((size_t)4 * P.n_active);
+    out.invm.resize((size_t)P.n_active);
+    long long marked = 0;
+#pragma omp parallel for schedule(static) reduction(+ : marked)
+    for (int n = 0; n < P.n_active; ++n) {
+        const int q0 = P.tptr[n], nt = P.tptr[n + 1] - q0;
+        int *s = &out.slot4[4 * (size_t)n];
+        for (int j = 0; j < 4; ++j) s[j] = j < nt ? P.tlist[q0 + j] : -1;
+        const float *c = &nc[4 * (size_t)n];
+        const bool mark = nt > 4 || P.dptr[n + 1] > P.dptr[n] || P.lptr[n + 1] > P.lptr[n] || c[2] != 0.f ||
+                          c[3] != 0.f || std::memcmp(&c[0], &c[1], sizeof(float)) != 0 || !(c[0] > 0.f);
+        marked += mark ? 1 : 0;
+        out.invm[n] = mark ? -1.f : c[0];
+    }
+    out.marked = marked;
+    return true;
+}
+
 bool build_pipe_pack(const Plan &P, const Tiles &T, int max_runs, PipePack &out, std::string &why) {
     out = PipePack();
     if (T.hmax >= (1 << 14)) { why = "tile halo over 16383 nodes"; return false; }

@@ -172,6 +172,23 @@ bool build_mma_tiles(const Plan &P, int tn, int emax_limit, MmaTiles &T, std::st
 // -2 a2 C (x, y).
 pvec<float> node_coef32(const Plan &P);
 
+// Fixed-size gather records of the FP32 direct gather: per active node its
+// first four element terms (tlist entries, in tlist order; -1 past the last)
+// and 1/m_full, so that a common node reads no list pointers, no node
+// coefficients and no DRM or anchor lists, and its term entries are one
+// 16-byte load with nothing before it in the gather chain.  A node with more
+// than four terms, DRM terms, anchored hanging nodes, a dashpot or unequal x
+// and y coefficients is marked by a negative invm and reads those parts from
+// the CSR lists and node coefficients (its terms past the fourth from
+// tlist[tptr[n] + 4 ...]).  nc is node_coef32(P).  Fails (false, with why)
+// when an entry would not fit 31 bits (2^28 elements or more).
+struct NodeSlots {
+    pvec<int> slot4;                   // 4 per active node
+    pvec<float> invm;                  // per active node: 1/m_full (x = y), or -1 on a marked node
+    long long marked = 0;              // marked nodes
+};
+bool build_node_slots(const Plan &P, const pvec<float> &nc, NodeSlots &out, std::string &why);
+
 // What the bulk-copy pipeline reads per tile, in the formats its kernel
 // decodes (all arrays of 32-bit words, every tile's part 16-byte aligned):
 //   hdr    4 per tile: halo nodes, terms, term-pack offset (16-byte units), runs

@@ -138,7 +138,11 @@ typedef struct exfem_opts {
                           3 = element products on the tensor cores (tcgen05
                           kind::tf32 in 3xTF32; needs nrhs a multiple of 16,
                           else the direct gather runs), 4 = the direct
-                          gather as a persistent grid (same results as 0)  */
+                          gather as a persistent grid (same results as 0),
+                          5 = the direct gather reading every node's terms
+                          through list pointers, which 0 and 4 do below
+                          50,000 active nodes, instead of fixed-size node
+                          records (same results as 0)                     */
     int index_bits;    /* FP32 direct gather: 0 = 32-bit indices when every
                           thread id and array index fits, else 64; 64 = always
                           64-bit (same results)                               */

@@ -208,6 +208,25 @@ int probe_mma_tiles(void *h, int tn, int emax, int *sizes, int *nptr, int *eptr,
     return 0;
 }
 
+// The direct gather's slot records (build_node_slots): slot4[4 * n_active]
+// and invm[n_active] when non-NULL; returns the marked node count, or -1
+// when the builder refuses the model.
+long long probe_node_slots(void *h, int *slot4, float *invm) {
+    Plan &p = *static_cast<Plan *>(h);
+    NodeSlots S;
+    if (!build_node_slots(p, node_coef32(p), S, g_err)) return -1;
+    if (slot4) std::memcpy(slot4, S.slot4.data(), S.slot4.size() * sizeof(int));
+    if (invm) std::memcpy(invm, S.invm.data(), S.invm.size() * sizeof(float));
+    return S.marked;
+}
+
+// The FP32 node coefficients (node_coef32): 4 per active node.
+void probe_node_coef32(void *h, float *out) {
+    Plan &p = *static_cast<Plan *>(h);
+    const pvec<float> nc = node_coef32(p);
+    std::memcpy(out, nc.data(), nc.size() * sizeof(float));
+}
+
 // The tensor-core step's B operand (tc_b_operand_q4): 256 floats, the tf32 hi
 // tile then the lo tile, in the K-major core-matrix layout.
 void probe_mma_btile(float *out) {

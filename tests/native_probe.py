@@ -70,6 +70,10 @@ def lib():
     L.probe_tile_runs.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     L.probe_mma_tiles.restype = C.c_int
     L.probe_mma_tiles.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 4
+    L.probe_node_slots.restype = C.c_longlong
+    L.probe_node_slots.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    L.probe_node_coef32.restype = None
+    L.probe_node_coef32.argtypes = [C.c_void_p, C.c_void_p]
     L.probe_mma_btile.restype = None
     L.probe_mma_btile.argtypes = [C.c_void_p]
     L.probe_plan_wave.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, d]
@@ -140,6 +144,20 @@ class PlanView:
         vp = lambda a: a.ctypes.data_as(C.c_void_p)
         assert L.probe_mma_tiles(self.h, tn, emax, sz, vp(nptr), vp(eptr), vp(elist), vp(tj)) == 0
         return nptr, eptr, elist[:nel], tj[:len(self.tlist)]
+
+    def node_slots(self):
+        """(slot4 (n_active, 4), invm, marked) of build_node_slots, and the
+        node coefficients (n_active, 4) of node_coef32."""
+        L = lib()
+        na = int(self.scalars[0])
+        slot4 = np.zeros((max(na, 1), 4), np.int32)
+        invm = np.zeros(max(na, 1), np.float32)
+        nc = np.zeros((max(na, 1), 4), np.float32)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        marked = L.probe_node_slots(self.h, vp(slot4), vp(invm))
+        assert marked >= 0
+        L.probe_node_coef32(self.h, vp(nc))
+        return slot4[:na], invm[:na], int(marked), nc[:na]
 
     def tile_runs(self, tn):
         """(rptr, runs (nruns, 2) as (first node, count)) of build_tiles."""

@@ -324,3 +324,29 @@ def test_tensor_core_b_operand_is_the_q4_stiffness():
             for k in range(8):
                 got = float(at(hi, 8 * part + n, k)) + float(at(lo, 8 * part + n, k))
                 assert abs(got - K[n, k]) <= 2.0 ** -21 * max(abs(K[n, k]), 1e-30), (part, n, k, got, K[n, k])
+
+
+def test_node_slot_records_hold_each_nodes_first_terms():
+    """build_node_slots (the direct gather's fixed-size node records): every
+    active node's first four tlist entries in order, -1 past its last; a node
+    is marked (invm -1) exactly when it has more than four terms, DRM terms,
+    anchored hanging nodes, a dashpot or unequal x/y coefficients, and an
+    unmarked node's invm is its 1/m_full bit for bit."""
+    m = workloads.build("canyon", scale=0.2, steps=4)
+    P = npb.PlanView(m)
+    slot4, invm, marked, nc = P.node_slots()
+    na = int(P.scalars[0])
+    tptr, tlist, dptr, lptr = P.tptr, P.tlist, P.dptr, P.lptr
+    cnt = np.diff(tptr[:na + 1])
+    for j in range(4):
+        has = cnt > j
+        assert np.array_equal(slot4[has, j], tlist[tptr[:na][has] + j])
+        assert np.all(slot4[~has, j] == -1)
+    want = ((cnt > 4) | (np.diff(dptr[:na + 1]) > 0) | (np.diff(lptr[:na + 1]) > 0) | (nc[:, 2] != 0) |
+            (nc[:, 3] != 0) | (nc[:, 0].view(np.uint32) != nc[:, 1].view(np.uint32)))
+    assert np.array_equal(invm < 0, want) and marked == int(want.sum())
+    assert np.all(invm[want] == -1.0)
+    assert np.array_equal(invm[~want].view(np.uint32), nc[~want, 0].view(np.uint32))
+    # the refined canyon has every kind of marked node, and most are unmarked
+    assert (cnt > 4).any() and (np.diff(dptr[:na + 1]) > 0).any() and (np.diff(lptr[:na + 1]) > 0).any()
+    assert (nc[:, 2] != 0).any() and marked < na // 4

@@ -470,3 +470,37 @@ def test_persistent_step_matches_the_direct_gather():
         assert np.array_equal(a, b)
         for r in range(m.problem.nrhs):
             assert np.array_equal(ua[r], ub[r]), r
+
+
+@pytest.mark.parametrize("nwaves,rpt", [(1, 0), (2, 0), (4, 0), (6, 0), (6, 1), (8, 2), (8, 4)])
+def test_node_slot_records_match_the_list_form(nwaves, rpt):
+    """The direct gather reads a common node's first four terms and 1/m_full
+    from its fixed-size slot record (variant 0) and a marked node's DRM terms,
+    extra terms, dashpot and anchors from the lists; variant 5 reads every
+    node through the lists.  Same terms in the same order: bit-identical
+    seismograms and final states, on a refined canyon (hanging nodes, anchors,
+    DRM layer, dashpots) at every kernel shape (term corners from econn up to
+    4 RHS, copies from 6; paired and split rows; 1, 2, 4 RHS per thread).
+    The records are used from 50,000 active nodes: this canyon has 59,682."""
+    m = workloads.build("canyon", scale=0.55, steps=80, save_every=2, waves=EIGHT_WAVES[:nwaves])
+    assert m.nnodes > 55000
+    kw = dict(rhs_per_thread=rpt) if rpt else {}
+    a, ua = run32(m, variant=0, **kw)
+    b, ub = run32(m, variant=5, **kw)
+    assert np.abs(a).max() > 0
+    assert np.array_equal(a, b)
+    for r in range(m.problem.nrhs):
+        assert np.array_equal(ua[r], ub[r]), r
+
+
+def test_node_slot_records_on_the_batched_valley_and_persistent_grid():
+    """The 64-RHS valley (plain layout, term corner copies) and the persistent
+    grid (variant 4, which also reads the slot records) against the list form."""
+    m = workloads.build("valley_batched", scale=0.2, steps=60, save_every=2)
+    assert m.nnodes > 55000
+    a, ua = run32(m, variant=5)
+    for v in (0, 4):
+        b, ub = run32(m, variant=v)
+        assert np.array_equal(a, b), v
+        for r in range(0, m.problem.nrhs, 9):
+            assert np.array_equal(ua[r], ub[r]), (v, r)
