@@ -630,6 +630,7 @@ void exfem_gpu_default_opts(exfem_opts *o) {
     o->wait_cycles = 0;
     o->tune = 0;
     o->drm_inline = 0;
+    o->serial_launch = 0;
 }
 
 int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts *opts, exfem_ctx **out) {
@@ -649,6 +650,10 @@ int exfem_gpu_create(const exfem_mesh *mesh, const exfem_problem *prob, const ex
     if (o.wait_cycles < 0) { g_create_err = "wait_cycles must be >= 0"; return EXFEM_E_ARG; }
     if (o.tune != 0 && o.tune != 1) { g_create_err = "tune must be 0 or 1"; return EXFEM_E_ARG; }
     if (o.drm_inline != 0 && o.drm_inline != 1) { g_create_err = "drm_inline must be 0 or 1"; return EXFEM_E_ARG; }
+    if (o.serial_launch != 0 && o.serial_launch != 1) {
+        g_create_err = "serial_launch must be 0 or 1";
+        return EXFEM_E_ARG;
+    }
     const int max_bt = o.precision == EXFEM_FP64 ? 256 : 512;   // the kernels' __launch_bounds__
     if (o.block_threads < 0 || o.block_threads > max_bt || (o.block_threads % 32) != 0) {
         g_create_err = "block_threads must be a multiple of 32 in [0, " + std::to_string(max_bt) + "]";

@@ -73,7 +73,8 @@ class Opts(C.Structure):
                 ("graph_steps", C.c_int), ("block_threads", C.c_int),
                 ("rhs_per_thread", C.c_int), ("reorder", C.c_int), ("check_every", C.c_int),
                 ("variant", C.c_int), ("index_bits", C.c_int), ("pad_rhs", C.c_int),
-                ("wait_cycles", C.c_int), ("tune", C.c_int), ("drm_inline", C.c_int)]
+                ("wait_cycles", C.c_int), ("tune", C.c_int), ("drm_inline", C.c_int),
+                ("serial_launch", C.c_int)]
 
 
 class ModelInfo(C.Structure):

@@ -176,6 +176,13 @@ typedef struct exfem_opts {
                           many requests stepping at once their kernels hide
                           that pass anyway, and the second streams measured
                           3% slower on a saturated burst).  Same results   */
+    int serial_launch; /* FP32 form: 0 = the direct gather's step kernel is
+                          launched as a programmatic dependent of the
+                          hanging/receiver pass before it (its blocks start
+                          while that pass runs, load the node records no
+                          kernel writes, then wait for it; default); 1 = it
+                          launches once that pass has finished.  Same
+                          results                                         */
 } exfem_opts;
 
 typedef struct exfem_ctx exfem_ctx;

@@ -56,8 +56,8 @@ def test_argument_errors_need_no_device():
     bad = default_opts(index_bits=32)   # 0 (automatic) or 64
     assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
     assert b"index_bits" in L.exfem_gpu_last_error(None)
-    assert default_opts().drm_inline == 0 and default_opts().tune == 0
-    for field, bad_value in (("drm_inline", 2), ("tune", 2)):
+    assert default_opts().drm_inline == 0 and default_opts().tune == 0 and default_opts().serial_launch == 0
+    for field, bad_value in (("drm_inline", 2), ("tune", 2), ("serial_launch", -1)):
         bad = default_opts(**{field: bad_value})
         assert L.exfem_gpu_create(C.byref(m), C.byref(p), C.byref(bad), C.byref(h)) == EXFEM_E_ARG
         assert field.encode() in L.exfem_gpu_last_error(None)

@@ -504,3 +504,20 @@ def test_node_slot_records_on_the_batched_valley_and_persistent_grid():
         assert np.array_equal(a, b), v
         for r in range(0, m.problem.nrhs, 9):
             assert np.array_equal(ua[r], ub[r]), (v, r)
+
+
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_programmatic_dependent_launch_keeps_results(use_graph):
+    """The direct gather's step kernel launches as a programmatic dependent of
+    the hanging/receiver pass before it (exfem_opts.serial_launch = 0, the
+    default): its blocks may start while that pass runs and wait for it before
+    touching the state.  Bit-identical to serial launches, with graph replay
+    and without, with the DRM forces inline and on the second stream, in the
+    slot and list forms and the persistent grid."""
+    m = workloads.build("canyon", scale=0.55, steps=70, save_every=2, waves=EIGHT_WAVES[:2])
+    for kw in (dict(), dict(drm_inline=1), dict(variant=5), dict(variant=4)):
+        a, ua = run32(m, use_graph=use_graph, serial_launch=1, **kw)
+        b, ub = run32(m, use_graph=use_graph, **kw)
+        assert np.array_equal(a, b), kw
+        for r in range(m.problem.nrhs):
+            assert np.array_equal(ua[r], ub[r]), (kw, r)
