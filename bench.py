@@ -290,19 +290,24 @@ def accuracy_leg(args, local, tuned):
     from util import peak_rel, per_receiver_rel
 
     def pair(m, kw32):
-        seis = {}
+        """Seismograms of both forms over the whole run, and each form's
+        device time per step (CUDA events around the run on its stream)."""
+        seis, us = {}, {}
         for prec in (1, 0):
             with Solver(m, precision=prec, device=local, **(kw32 if prec == 1 else {})) as s:
                 s.init_explicit()
-                s.run()
+                ms = C.c_double(0)
+                if s.lib.exfem_gpu_run_timed(s.h, m.problem.nsteps, C.byref(ms)) != 0:
+                    raise RuntimeError("timed run failed")
                 s.sync()
                 seis[prec] = s.seismograms()
-        return seis
+                us[prec] = 1000.0 * ms.value / m.problem.nsteps
+        return seis, us
 
     out = {"against": "plain FP64 GPU form (matches the oracle to 1e-12)", "tolerance": 1e-4}
     if args.accuracy_batched_steps > 0:
         mb = workloads.build(args.workload, scale=args.scale, steps=args.accuracy_batched_steps)
-        seis = pair(mb, tuned)
+        seis, _ = pair(mb, tuned)
         l2 = [float(per_receiver_rel(seis[1][r], seis[0][r]).max()) for r in range(mb.problem.nrhs)]
         pk = [float(peak_rel(seis[1][r], seis[0][r]).max()) for r in range(mb.problem.nrhs)]
         out.update({"workload": args.workload, "elements": mb.nelems, "rhs": mb.problem.nrhs,
@@ -311,11 +316,13 @@ def accuracy_leg(args, local, tuned):
                     "worst_rhs": int(np.argmax(l2))})
     if args.accuracy_steps > 0:
         m = workloads.build("valley", scale=args.scale, steps=args.accuracy_steps)
-        seis = pair(m, {})
+        seis, us = pair(m, {})
         out["valley_full_length"] = {
             "workload": "valley", "elements": m.nelems, "rhs": m.problem.nrhs, "steps": m.problem.nsteps,
             "max_rel_l2": float(per_receiver_rel(seis[1][0], seis[0][0]).max()),
-            "max_peak_rel": float(peak_rel(seis[1][0], seis[0][0]).max())}
+            "max_peak_rel": float(peak_rel(seis[1][0], seis[0][0]).max()),
+            "fp32_us_per_step": round(us[1], 2), "fp64_us_per_step": round(us[0], 2),
+            "timing": "device time of the whole run (CUDA events on the context's stream), default shapes"}
     return out
 
 

@@ -2,10 +2,11 @@
 //
 // It times every candidate shape of the FP32 form on the caller's own model
 // and keeps the fastest: kernel variant (0 direct gather, 4 the same as a
-// persistent grid, 1 shared-memory tiles, 2 bulk-copy pipeline when nrhs is
-// a multiple of 4, 3 tensor-core step when nrhs is a multiple of 16), block
-// size (128, 256, 512) and
-// right-hand sides per thread (1, 2, 4 dividing nrhs).
+// persistent grid, 5 the direct gather in its list form from 50,000 nodes,
+// where 0 reads fixed-size node records, 1 shared-memory tiles, 2 bulk-copy
+// pipeline when nrhs is a multiple of 4, 3 tensor-core step when nrhs is a
+// multiple of 16), block size (128, 256, 512) and right-hand sides per
+// thread (1, 2, 4 dividing nrhs).
 // Each candidate gets its own context (exfem_gpu_create with that shape), a
 // few warm-up steps, and a burst timed with CUDA events on the context's
 // stream (exfem_gpu_run_timed).  Results are cached in the process per
@@ -19,6 +20,7 @@
 #include <tuple>
 #include <vector>
 
+#include "exfem_ctx.h"
 #include "exfem_gpu.h"
 #include "exfem_plan.h"
 
@@ -38,14 +40,37 @@ struct TuneVal {
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneVal> g_tune_cache;
 
-// Times `steps` steps after `warmup` of one candidate; < 0 when the
-// candidate cannot run (unsupported shape, out of memory, failed step).
+// Steps per captured graph (exfem_gpu_run's rule).
+int graph_len(const exfem_opts &o) {
+    int g = o.graph_steps > 0 ? o.graph_steps : 16;
+    return g + (g & 1);
+}
+
+// Steps a candidate runs before its timed steps: `warmup` and one graph's
+// worth, rounded up to an even count, so that the graph is captured and
+// instantiated before the clock starts and the timed steps begin at the
+// parity it was captured from.
+int pre_steps(const exfem_opts &o, int warmup) {
+    const int n = warmup + (o.use_graph ? graph_len(o) : 0);
+    return n + (n & 1);
+}
+
+// The timed steps: `steps` rounded up to whole graph replays, so the timing
+// is of replays only (as a long run is), not of single-step launches.
+int timed_steps(const exfem_opts &o, int steps) {
+    if (!o.use_graph) return steps;
+    const int g = graph_len(o);
+    return std::max(g, (steps + g - 1) / g * g);
+}
+
+// Times `steps` steps after pre_steps(o, warmup) of one candidate; < 0 when
+// the candidate cannot run (unsupported shape, out of memory, failed step).
 double time_candidate(const exfem_mesh *mesh, const exfem_problem *prob, const exfem_opts &o, int warmup,
                       int steps) {
     exfem_ctx *ctx = nullptr;
     if (exfem_gpu_create(mesh, prob, &o, &ctx) != EXFEM_OK) return -1.0;
     double ms = -1.0;
-    if (exfem_gpu_init_explicit(ctx, nullptr) == EXFEM_OK && exfem_gpu_run(ctx, warmup) == EXFEM_OK &&
+    if (exfem_gpu_init_explicit(ctx, nullptr) == EXFEM_OK && exfem_gpu_run(ctx, pre_steps(o, warmup)) == EXFEM_OK &&
         exfem_gpu_sync(ctx) == EXFEM_OK) {
         double t = 0.0;
         if (exfem_gpu_run_timed(ctx, steps, &t) == EXFEM_OK && exfem_gpu_sync(ctx) == EXFEM_OK) ms = t / steps;
@@ -81,9 +106,11 @@ int autotune_shapes(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opt
     }
     const int warmup = 3;
     exfem_problem p = *prob;   // enough steps for the timing, whatever the problem's length
-    p.nsteps = warmup + steps;
+    const int tsteps = timed_steps(*opts, steps);
+    p.nsteps = pre_steps(*opts, warmup) + tsteps;
     if (p.io_interval < 1) p.io_interval = 1;
     std::vector<int> variants = {0, 4};
+    if (mesh->nnodes >= kSlotMinNodes) variants.push_back(5);
     if (max_variant >= 1) variants.push_back(1);
     if (max_variant >= 2 && R % 4 == 0) variants.push_back(2);
     if (max_variant >= 3 && R % 16 == 0) variants.push_back(3);
@@ -97,7 +124,7 @@ int autotune_shapes(const exfem_mesh *mesh, const exfem_problem *prob, exfem_opt
                 o.variant = v;
                 o.block_threads = bt;
                 o.rhs_per_thread = rpt;
-                const double ms = time_candidate(mesh, &p, o, warmup, steps);
+                const double ms = time_candidate(mesh, &p, o, warmup, tsteps);
                 if (ms > 0.0 && (best.variant < 0 || ms < best.ms_per_step)) best = TuneVal{v, bt, rpt, ms};
             }
         }

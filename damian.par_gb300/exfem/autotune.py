@@ -1,10 +1,12 @@
 """Autotuner for the FP32 step kernel: a binding of exfem_gpu_autotune.
 
 The library times every candidate (kernel variant, block size, right-hand
-sides per thread) on the real model — variant 0 is the direct gather, 1 the
-shared-memory tiled kernel, 2 the persistent kernel fed by bulk copies (when
-nrhs is a multiple of 4) — each in a context of its own, with CUDA events on
-its stream, and keeps the fastest.  Results are cached in the process per
+sides per thread) on the real model — variant 0 is the direct gather, 4 the
+same as a persistent grid, 5 its list form (from 50,000 nodes, where 0 reads
+fixed-size node records), 1 the shared-memory tiled kernel, 2 the persistent
+kernel fed by bulk copies (when nrhs is a multiple of 4), 3 the tensor-core
+step (when nrhs is a multiple of 16) — each in a context of its own, with
+CUDA events on its stream, and keeps the fastest.  Results are cached in the process per
 (elements, nodes, rhs, device), inside the library, so a Fortran host or the
 server gets the same shapes as this module.
 """
