@@ -573,7 +573,8 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="force the step kernel's block size")
     ap.add_argument("--rpt", type=int, default=0, help="force right-hand sides per thread")
     ap.add_argument("--variant", type=int, default=-1, help="force the kernel variant (FP32: 0 direct gather, 1 shared-memory tiles, 2 bulk-copy "
-                         "pipeline; FP64: 0 reference order, 1 closed form)")
+                         "pipeline, 3 tensor-core step, 4 persistent direct gather, 5 list-form direct gather; "
+                         "FP64: 0 reference order, 1 closed form)")
     ap.add_argument("--serve-requests", type=int, default=32, help="requests in the serving sample (0: skip)")
     ap.add_argument("--serve-burst", type=int, default=16, help="requests in the saturated serving sample (0: skip)")
     ap.add_argument("--burst-request", type=int, default=-1,
