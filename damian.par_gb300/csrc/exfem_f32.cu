@@ -360,6 +360,28 @@ __global__ void k_term_corners(const int *__restrict__ tlist, const int *__restr
     reinterpret_cast<int4 *>(tcorn)[q] = __ldg(reinterpret_cast<const int4 *>(econn) + e);
 }
 
+// The direct gather's node slot records (build_node_slots, in the same
+// words): per active node its first four tlist entries (-1 past the last)
+// and 1/m_full, or -1 on a node with more than four terms, DRM terms,
+// anchored hanging nodes, a dashpot or unequal x and y coefficients.
+__global__ void k_node_slots(const int *__restrict__ tptr, const int *__restrict__ tlist, const int *__restrict__ dptr,
+                             const int *__restrict__ lptr, const float *__restrict__ ncoef4, int n_active,
+                             int *__restrict__ slot4, float *__restrict__ invm) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= n_active) return;
+    const int q0 = tptr[n], nt = tptr[n + 1] - q0;
+    int4 s;
+    s.x = nt > 0 ? tlist[q0] : -1;
+    s.y = nt > 1 ? tlist[q0 + 1] : -1;
+    s.z = nt > 2 ? tlist[q0 + 2] : -1;
+    s.w = nt > 3 ? tlist[q0 + 3] : -1;
+    reinterpret_cast<int4 *>(slot4)[n] = s;
+    const float4 c = reinterpret_cast<const float4 *>(ncoef4)[n];
+    const bool mark = nt > 4 || dptr[n + 1] > dptr[n] || lptr[n + 1] > lptr[n] || c.z != 0.f || c.w != 0.f ||
+                      __float_as_uint(c.x) != __float_as_uint(c.y) || !(c.x > 0.f);
+    invm[n] = mark ? -1.f : c.x;
+}
+
 // The slot form's corner copies: for slot j of active node n (an entry, or
 // -1), the four corners of its element at tcorn4[4 * (4n + j)], from the slot
 // records and the element corners (an empty slot gets -1s, never read).
@@ -1750,10 +1772,18 @@ int f32_alloc(Ctx &c) {
     m.ninvm = nullptr;
     m.tcorn4 = nullptr;
     if (direct && c.opts.variant != 5 && P.n_active >= kSlotMinNodes) {
-        NodeSlots S;
-        std::string why;
-        if (build_node_slots(P, nc, S, why)) {
-            if ((rc = upload32(c, S.slot4, &m.tslot4)) || (rc = upload32(c, S.invm, &m.ninvm))) return rc;
+        // built on the device from the lists and node coefficients already
+        // there (build_node_slots states the same records on the host)
+        if ((long long)P.ne * 8 <= (1ll << 31) - 1 && P.n_active > 0) {
+            int *s4 = nullptr;
+            float *iv = nullptr;
+            if ((rc = alloc32(c, 4 * (size_t)P.n_active, &s4)) || (rc = alloc32(c, (size_t)P.n_active, &iv))) return rc;
+            k_node_slots<<<nblocks(P.n_active, 256), 256, 0, c.stream>>>(m.tptr, m.tlist, m.dptr, m.lptr, m.ncoef4,
+                                                                        P.n_active, s4, iv);
+            c.launches++;
+            CK(cudaGetLastError());
+            m.tslot4 = s4;
+            m.ninvm = iv;
             if (f32_slot_corners(P.R)) {
                 const long long ns4 = 4 * (long long)P.n_active;
                 int *tc = nullptr;
