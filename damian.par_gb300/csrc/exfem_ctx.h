@@ -31,7 +31,8 @@ struct DevModel {
     double worigin_x, worigin_y;
     const int *econn;        // 4 per element
     const double *ecoef;     // 4 per element (FP64)
-    const float *ecoef32;    // 4 per element (FP32)
+    const float *ecoef32;    // 4 per element (FP32), derived from ecoef2 (fp32_coef)
+    const float *ecoef2;     // 2 per element: lam/12, mu/4 (FP32)
     const double *ekv;       // 6 per element: calck_values(mu, lambda)
     const double *emass;     // per element
     const int *edamp;        // per element, -1 or slot

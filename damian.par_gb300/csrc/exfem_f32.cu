@@ -360,6 +360,21 @@ __global__ void k_term_corners(const int *__restrict__ tlist, const int *__restr
     reinterpret_cast<int4 *>(tcorn)[q] = __ldg(reinterpret_cast<const int4 *>(econn) + e);
 }
 
+// An element's four FP32 coefficients from its two stored values, with the
+// operations and roundings of fp32_coef (exfem_plan.h).
+__device__ __forceinline__ float4 coef_from2(float2 k2) {
+    const float B = __fmul_rn(3.f, k2.x);
+    return make_float4(__fadd_rn(B, __fmul_rn(2.f, k2.y)), B, k2.y, __fadd_rn(k2.x, k2.y));
+}
+
+// ecoef32 from ecoef2, once per context (8 bytes per element uploaded
+// instead of 16).
+__global__ void k_coef32(const float *__restrict__ ecoef2, float *__restrict__ ecoef32, int ne) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    reinterpret_cast<float4 *>(ecoef32)[e] = coef_from2(reinterpret_cast<const float2 *>(ecoef2)[e]);
+}
+
 // The direct gather's node slot records (build_node_slots, in the same
 // words): per active node its first four tlist entries (-1 past the last)
 // and 1/m_full, or -1 on a node with more than four terms, DRM terms,
@@ -477,13 +492,12 @@ __device__ __forceinline__ void node_update(const DevModel &m, int n, I bn, I R,
 // One element term of a node's gather: -K_e u_e at the node's corner c of
 // element e (weight 1/2 for a hanging node's term carried by its anchor),
 // ent = ((e*4 + c) << 1) | half, cn = the element's corners.
+// k: the element's coefficients (ecoef32, or coef_from2 of ecoef2).
 template <int RPT, bool PAIR, typename I>
-__device__ __forceinline__ void gather_term(const DevModel &m, int ent, int4 cn, I R, I roff,
-                                            const float *__restrict__ uh, float (&ax)[RPT], float (&ay)[RPT]) {
+__device__ __forceinline__ void gather_term(int ent, int4 cn, float4 k, I R, I roff, const float *__restrict__ uh,
+                                            float (&ax)[RPT], float (&ay)[RPT]) {
     float w = (ent & 1) ? 0.5f : 1.0f;
-    int ec = ent >> 1;
-    int e = ec >> 2, c = ec & 3;
-    float4 k = __ldg(reinterpret_cast<const float4 *>(m.ecoef32) + e);
+    int c = (ent >> 1) & 3;
     const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
     float ux[4][RPT], uy[4][RPT];
 #pragma unroll
@@ -611,25 +625,29 @@ __device__ __forceinline__ void step32_tile(const DevModel &m, unsigned tile, co
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (sl[j] < 0) continue;   // only trailing slots are empty
+            const int e = (sl[j] >> 1) >> 2;
             int4 cn;
             if constexpr (TC) cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn4) + ((I)n * 4 + j));
-            else cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + ((sl[j] >> 1) >> 2));
-            gather_term<RPT, PAIR, I>(m, sl[j], cn, R, roff, uh, ax, ay);
+            else cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + e);
+            // the two stored coefficients (8 B per element, not 16)
+            const float4 k = coef_from2(__ldg(reinterpret_cast<const float2 *>(m.ecoef2) + e));
+            gather_term<RPT, PAIR, I>(sl[j], cn, k, R, roff, uh, ax, ay);
         }
         if (invm < 0.f) {
             for (int q = m.tptr[n] + 4; q < m.tptr[n + 1]; ++q) {
-                const int ent = __ldg(m.tlist + q);
-                gather_term<RPT, PAIR, I>(m, ent, __ldg(reinterpret_cast<const int4 *>(m.econn) + ((ent >> 1) >> 2)),
-                                          R, roff, uh, ax, ay);
+                const int ent = __ldg(m.tlist + q), e = (ent >> 1) >> 2;
+                gather_term<RPT, PAIR, I>(ent, __ldg(reinterpret_cast<const int4 *>(m.econn) + e),
+                                          __ldg(reinterpret_cast<const float4 *>(m.ecoef32) + e), R, roff, uh, ax, ay);
             }
         }
     } else {
         for (int q = m.tptr[n]; q < m.tptr[n + 1]; ++q) {
-            int ent = __ldg(m.tlist + q);
+            const int ent = __ldg(m.tlist + q), e = (ent >> 1) >> 2;
             int4 cn;
             if constexpr (TC) cn = __ldg(reinterpret_cast<const int4 *>(m.tcorn) + q);
-            else cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + ((ent >> 1) >> 2));
-            gather_term<RPT, PAIR, I>(m, ent, cn, R, roff, uh, ax, ay);
+            else cn = __ldg(reinterpret_cast<const int4 *>(m.econn) + e);
+            gather_term<RPT, PAIR, I>(ent, cn, __ldg(reinterpret_cast<const float4 *>(m.ecoef32) + e), R, roff, uh,
+                                      ax, ay);
         }
     }
     node_update<RPT, PAIR, I, SLOT>(m, n, bn, R, roff, ax, ay, uh, uhn, uc, dh, dc, invm);
@@ -1655,7 +1673,19 @@ int f32_alloc(Ctx &c) {
     int rc;
     if ((rc = upload32(c, nc, &m.ncoef4))) return rc;
     if ((rc = upload32(c, hc, &m.hcoef4))) return rc;
-    if ((rc = upload32(c, P.ecoef32, &m.ecoef32))) return rc;
+    // the FP32 coefficients: two per element uploaded, the four derived on
+    // the device (the same operations as the plan's ecoef32)
+    if ((rc = upload32(c, P.ecoef2, &m.ecoef2))) return rc;
+    {
+        float *k4 = nullptr;
+        if ((rc = alloc32(c, 4 * (size_t)std::max(P.ne, 1), &k4))) return rc;
+        if (P.ne > 0) {
+            k_coef32<<<nblocks(P.ne, 256), 256, 0, c.stream>>>(m.ecoef2, k4, P.ne);
+            c.launches++;
+            CK(cudaGetLastError());
+        }
+        m.ecoef32 = k4;
+    }
     // with few right-hand sides the next step's DRM forces run beside this
     // step on a second stream, into the other of two force slots
     c.drm_side = m.ns > 0 && P.R <= kDrmSideMaxRhs && c.opts.drm_inline == 0;

@@ -1019,7 +1019,7 @@ size_t exfem_gpu_estimate_bytes(const exfem_mesh *mesh, const exfem_problem *pro
         const size_t H = nn + 16 * (ne + nh) + nh;
         b += 8 * (nn + 2) + 12 * H + 8 * (4 * ne + 4 * nh) + 4 * nn + 4 * nh;
     }
-    if (!f64) b += 20 * nn;                                         // node slot records (4 entries, 1/m_full)
+    if (!f64) b += 20 * nn + 8 * ne;                                // node slot records, the two stored coefficients
     // the direct gather's term corners: per term (list form) or 4 per node (slot records)
     if (!f64 && (f32_term_corners(R) || f32_slot_corners(R))) b += std::max(16 * (4 * ne + 4 * nh), 64 * nn);
     if (prob->point_kind) b += nn + 4 * (size_t)std::max(prob->npoint, 0) + 1024;   // source flags and nodes

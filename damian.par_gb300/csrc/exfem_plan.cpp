@@ -458,6 +458,7 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
     // ---- per-element data (internal order); dashpot slots numbered in that order
     P.econn.resize((size_t)ne * 4);
     P.ecoef32.resize((size_t)ne * 4);
+    P.ecoef2.resize((size_t)ne * 2);
     P.emass.resize(ne);
     if (fp64_operator) {
         P.ecoef.resize((size_t)ne * 4);
@@ -485,9 +486,12 @@ int build_plan(const exfem_mesh &mesh, const exfem_problem &prob, bool reorder, 
         damped[ie] = 0;
         if (!(h > 0) || !(rho > 0)) { bad_elem = std::min(bad_elem, e); continue; }
         eh[ie] = h;
-        // the closed form's coefficients, in FP64, and rounded once for FP32
+        // the closed form's coefficients in FP64, and the FP32 form's two
+        // stored values and the four it derives from them (fp32_coef)
         const double co[4] = {(lam + 2.0 * mu) / 4.0, lam / 4.0, mu / 4.0, (lam + 3.0 * mu) / 12.0};
-        for (int k = 0; k < 4; ++k) P.ecoef32[(size_t)ie * 4 + k] = (float)co[k];
+        P.ecoef2[(size_t)ie * 2] = (float)(lam / 12.0);
+        P.ecoef2[(size_t)ie * 2 + 1] = (float)(mu / 4.0);
+        fp32_coef(P.ecoef2[(size_t)ie * 2], P.ecoef2[(size_t)ie * 2 + 1], &P.ecoef32[(size_t)ie * 4]);
         if (fp64_operator) {
             P.emulam[(size_t)ie * 2] = mu;
             P.emulam[(size_t)ie * 2 + 1] = lam;

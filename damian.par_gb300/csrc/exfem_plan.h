@@ -55,6 +55,21 @@ int init_wave_const(const exfem_wave &w, double alpha, double beta, WaveConst &o
 // The six distinct magnitudes of calck(mu, lambda) (formulation.f90:276-313),
 // each with the formula's operations: (3m+l)/3, (m+l)/4, (3m+2l)/6, (m-l)/4,
 // (3m+l)/6, l/6.  The FP64 kernels rebuild K from them with signs.
+// The FP32 form's four closed-form coefficients ((l+2m)/4, l/4, m/4,
+// (l+3m)/12) from its two stored values b3 = l/12 and c = m/4 (FP32, each
+// rounded once): B = 3 b3, A = B + 2c, D = b3 + c, each an FP32 operation
+// rounded once (no contraction).  The four are linear in (lambda, mu), so an
+// element needs only the two values; each result is within 2 ulps of its
+// FP64 value rounded once.  The device computes the same operations.
+inline void fp32_coef(float b3, float c, float out[4]) {
+    volatile float B = 3.0f * b3;   // separate roundings on every compiler
+    volatile float c2 = 2.0f * c;
+    out[1] = B;
+    out[0] = B + c2;
+    out[2] = c;
+    out[3] = b3 + c;
+}
+
 inline void calck_values(double m, double l, double kv[6]) {
     kv[0] = (3.0 * m + l) / 3.0;
     kv[1] = (m + l) / 4.0;
@@ -77,7 +92,8 @@ struct Plan {
     // elements (internal order)
     pvec<int> econn;                // 4 per element: internal node ids of the non-hanging corners
     pvec<double> ecoef;             // 4 per element: (lam+2mu)/4, lam/4, mu/4, (lam+3mu)/12
-    pvec<float> ecoef32;            // same, FP32
+    pvec<float> ecoef32;            // same, FP32, from ecoef2 (fp32_coef)
+    pvec<float> ecoef2;             // 2 per element: lam/12 and mu/4, each rounded once to FP32
     pvec<double> emulam;            // 2 per element: (mu, lambda)
     pvec<double> ekv;               // 6 per element: calck_values(mu, lambda)
     pvec<double> emass;             // rho*(h/2)^2 per element (getmassof)

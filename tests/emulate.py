@@ -142,7 +142,7 @@ def emulate_fp32(model, nsteps, rhs=0, comp="bf16"):
     rnd = bf16 if comp == "bf16" else (lambda v: np.asarray(v, f32))
     econn = P.econn.reshape(-1, 4)
     ecoef = P.ecoef.reshape(-1, 4)
-    k32 = ecoef.astype(f32)
+    k32 = np.asarray(P.ecoef32).reshape(-1, 4)   # the kernels' FP32 coefficients
     emass = P.emass
     nodes = model.nodes()[P.ref_of_node]
     worigin = np.array(model.problem.worigin[:])

@@ -153,7 +153,7 @@ long long probe_plan_size(void *h, const char *name) {
     SZ(ref_of_node) SZ(node_of_ref) SZ(ref_of_elem) SZ(econn) SZ(ecoef) SZ(emass) SZ(edamp) SZ(edampv)
     SZ(tptr) SZ(tlist) SZ(dptr) SZ(dlist) SZ(mfull_ref) SZ(inv_mfull) SZ(nmass) SZ(ndamp) SZ(hang)
     SZ(s_elem) SZ(s_kind) SZ(rnode) SZ(rw) SZ(rsoil) SZ(rxy) SZ(lptr) SZ(llist) SZ(ownptr) SZ(ownlist)
-    SZ(ecoef32) SZ(emulam) SZ(mfull_int) SZ(elem_of_ref) SZ(nxy) SZ(odptr) SZ(odlist)
+    SZ(ecoef32) SZ(ecoef2) SZ(emulam) SZ(mfull_int) SZ(elem_of_ref) SZ(nxy) SZ(odptr) SZ(odlist)
 #undef SZ
     if (n == "scalars") return 8;
     return -1;
@@ -166,7 +166,7 @@ int probe_plan_copy(void *h, const char *name, void *out) {
     CP(ref_of_node) CP(node_of_ref) CP(ref_of_elem) CP(econn) CP(ecoef) CP(emass) CP(edamp) CP(edampv)
     CP(tptr) CP(tlist) CP(dptr) CP(dlist) CP(mfull_ref) CP(inv_mfull) CP(nmass) CP(ndamp) CP(hang)
     CP(s_elem) CP(s_kind) CP(rnode) CP(rw) CP(rsoil) CP(rxy) CP(lptr) CP(llist) CP(ownptr) CP(ownlist)
-    CP(ecoef32) CP(emulam) CP(mfull_int) CP(elem_of_ref) CP(nxy) CP(odptr) CP(odlist)
+    CP(ecoef32) CP(ecoef2) CP(emulam) CP(mfull_int) CP(elem_of_ref) CP(nxy) CP(odptr) CP(odlist)
 #undef CP
     if (n == "scalars") {
         double *d = static_cast<double *>(out);

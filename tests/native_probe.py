@@ -88,7 +88,7 @@ def dp(a):
 INT_FIELDS = {"ref_of_node", "node_of_ref", "ref_of_elem", "econn", "edamp", "tptr", "tlist", "dptr", "dlist",
               "hang", "s_elem", "s_kind", "rnode", "rsoil", "lptr", "llist", "ownptr", "ownlist", "elem_of_ref",
               "odptr", "odlist"}
-FLOAT32_FIELDS = {"ecoef32"}
+FLOAT32_FIELDS = {"ecoef32", "ecoef2"}
 
 
 class PlanView:

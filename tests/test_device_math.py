@@ -239,7 +239,7 @@ def test_pipeline_records_decode_to_the_mesh(name, tn):
     hptr, hlist, tslot, nslot, lslot, hmax = P.tiles(tn)
     hdr, runs, nrec, tpack, tmax = P.pipe_pack(tn)
     econn = P.econn.reshape(-1, 4)
-    ecoef = np.asarray(P.ecoef, np.float64).reshape(-1, 4).astype(np.float32)
+    ecoef = np.asarray(P.ecoef32).reshape(-1, 4)
     tp = tpack.view(np.uint32)
     for n in range(na):
         t = n // tn

@@ -6,7 +6,9 @@ then each node's entries ordered by reference element), CSR pointers by
 chunked prefix sums, the dashpot slot numbering and the first-error
 reductions.  Every array must be the same whatever the thread count, and the
 same as the single-threaded builder it replaced: the digests below were taken
-from that builder on the same decks.
+from that builder on the same decks, over every array but the FP32 element
+coefficients, whose definition changed after it (two stored values, the four
+derived from them: test_fp32_coefficients_derive_from_two_values).
 """
 import hashlib
 import os
@@ -17,20 +19,20 @@ import pytest
 import native_probe as npb
 from exfem import workloads
 
-FIELDS = ["ref_of_node", "node_of_ref", "ref_of_elem", "elem_of_ref", "econn", "ecoef", "ecoef32", "emulam",
+FIELDS = ["ref_of_node", "node_of_ref", "ref_of_elem", "elem_of_ref", "econn", "ecoef", "emulam",
           "emass", "edamp", "edampv", "tptr", "tlist", "dptr", "dlist", "mfull_ref", "inv_mfull", "mfull_int",
           "nmass", "ndamp", "hang", "s_elem", "s_kind", "rnode", "rw", "rsoil", "rxy", "lptr", "llist",
           "ownptr", "ownlist", "odptr", "odlist", "nxy", "scalars"]
 
 # (workload, kwargs) -> digest of the single-threaded builder's arrays
 CASES = {
-    "valley_batched": (dict(scale=0.12, steps=20), "26a6c1bfb9cabadc"),
-    "canyon": (dict(scale=0.2, steps=10), "fa53144bef79ac0b"),
-    "point_source": (dict(scale=0.5, steps=10, kind="POINTD"), "4e235952da0c6b34"),
-    "homogeneous_rectangle": (dict(scale=0.5, steps=10), "4b81df71342c039c"),
+    "valley_batched": (dict(scale=0.12, steps=20), "e8ae93a9acd63b93"),
+    "canyon": (dict(scale=0.2, steps=10), "6a605c372974b03d"),
+    "point_source": (dict(scale=0.5, steps=10, kind="POINTD"), "5c5796d8eeab0f67"),
+    "homogeneous_rectangle": (dict(scale=0.5, steps=10), "7233fd701507a698"),
     # large enough for several sort and prefix-sum chunks per pass
-    "valley": (dict(scale=0.45, steps=10), "bf51c2b72f8a59f6"),
-    "canyon@large": (dict(scale=0.9, steps=10), "b96363ed79b27238"),
+    "valley": (dict(scale=0.45, steps=10), "b75f38965511ea6c"),
+    "canyon@large": (dict(scale=0.9, steps=10), "5d5f7462b2b92b59"),
 }
 
 
@@ -81,3 +83,27 @@ def test_plan_errors_name_the_first_bad_element():
     h = L.probe_plan(m.mesh, m.problem, 1)
     assert h
     L.probe_plan_free(h)
+
+
+def test_fp32_coefficients_derive_from_two_values():
+    """The FP32 form stores two values per element, lambda/12 and mu/4, each
+    rounded once from FP64, and derives its four closed-form coefficients from
+    them with single FP32 operations (fp32_coef, exfem_plan.h; the device's
+    coef_from2 does the same): B = 3 b3, A = B + 2 c, D = b3 + c.  Each is
+    within 2 ulps of its FP64 value ((l+2m)/4, l/4, m/4, (l+3m)/12)."""
+    f = np.float32
+    for name in ("valley", "canyon"):
+        m = workloads.build(name, scale=0.3, steps=4)
+        P = npb.PlanView(m)
+        e2 = np.asarray(P.ecoef2).reshape(-1, 2)
+        e4 = np.asarray(P.ecoef32).reshape(-1, 4)
+        mulam = np.asarray(P.emulam).reshape(-1, 2)
+        mu, lam = mulam[:, 0], mulam[:, 1]
+        assert np.array_equal(e2[:, 0], (lam / 12.0).astype(f)) and np.array_equal(e2[:, 1], (mu / 4.0).astype(f))
+        B = f(3) * e2[:, 0]
+        want = np.stack([B + f(2) * e2[:, 1], B, e2[:, 1], e2[:, 0] + e2[:, 1]], axis=1)
+        assert np.array_equal(e4, want)
+        exact = np.stack([(lam + 2 * mu) / 4, lam / 4, mu / 4, (lam + 3 * mu) / 12], axis=1)
+        ulp = np.spacing(exact.astype(f)).astype(np.float64)
+        assert np.all(np.abs(e4.astype(np.float64) - exact) <= 2 * ulp)
+        assert np.array_equal(np.asarray(P.ecoef).reshape(-1, 4), exact)
