@@ -176,10 +176,14 @@ inline int spread_blocks(long long items, int per_block) {
 // four (0.55M-element valley); the copy is 1-2% faster from six.
 constexpr bool f32_term_corners(int R) { return R > 4; }
 // The same choice for the fixed-size node records (4 x 16 B per node in
-// tcorn4).  Measured with the records on the 1.5M-element valley at one RHS
-// and on 0.52M- and 0.86M-element requests at two: copies at every R were
-// 10-27% slower than econn up to four RHS.
-constexpr bool f32_slot_corners(int R) { return R > 4; }
+// tcorn4).  With the records the chain without copies is slot record ->
+// econn -> corner rows, one level longer, but the copies are most of a
+// node's metadata.  Measured: copies 10-27% slower up to four RHS (the
+// 1.5M-element valley at one, 0.52M- and 0.86M-element requests at two);
+// econn 2-5% faster on the 6-, 8- and 12-RHS requests of the saturated burst
+// and the 6-RHS canyon (0.6% less for the burst's requests alone, 0.5% on
+// its makespan), and the copies 0.4-1.5% faster at 16.
+constexpr bool f32_slot_corners(int R) { return R > 12; }
 
 // FP32 direct gather: active nodes from which the fixed-size node records
 // (build_node_slots) replace the list form.  A marked node's path is longer

@@ -472,17 +472,22 @@ def test_persistent_step_matches_the_direct_gather():
             assert np.array_equal(ua[r], ub[r]), r
 
 
-@pytest.mark.parametrize("nwaves,rpt", [(1, 0), (2, 0), (4, 0), (6, 0), (6, 1), (8, 2), (8, 4)])
+SIXTEEN_WAVES = EIGHT_WAVES + [("WAVEP", 10.0), ("WAVEP", 30.0), ("WAVEP", 50.0), ("WAVEP", 70.0),
+                               ("WAVESV", 5.0), ("WAVESV", 15.0), ("WAVESV", 22.0), ("WAVESV", 28.0)]
+
+
+@pytest.mark.parametrize("nwaves,rpt", [(1, 0), (2, 0), (4, 0), (6, 0), (6, 1), (8, 2), (8, 4), (16, 0), (16, 2)])
 def test_node_slot_records_match_the_list_form(nwaves, rpt):
     """The direct gather reads a common node's first four terms and 1/m_full
     from its fixed-size slot record (variant 0) and a marked node's DRM terms,
     extra terms, dashpot and anchors from the lists; variant 5 reads every
     node through the lists.  Same terms in the same order: bit-identical
     seismograms and final states, on a refined canyon (hanging nodes, anchors,
-    DRM layer, dashpots) at every kernel shape (term corners from econn up to
-    4 RHS, copies from 6; paired and split rows; 1, 2, 4 RHS per thread).
-    The records are used from 50,000 active nodes: this canyon has 59,682."""
-    m = workloads.build("canyon", scale=0.55, steps=80, save_every=2, waves=EIGHT_WAVES[:nwaves])
+    DRM layer, dashpots) at every kernel shape (the slot form's term corners
+    from econn up to 12 RHS, copies from 14, the list form's copies from 6;
+    paired and split rows; 1, 2, 4 RHS per thread).  The records are used
+    from 50,000 active nodes: this canyon has 59,682."""
+    m = workloads.build("canyon", scale=0.55, steps=80, save_every=2, waves=SIXTEEN_WAVES[:nwaves])
     assert m.nnodes > 55000
     kw = dict(rhs_per_thread=rpt) if rpt else {}
     a, ua = run32(m, variant=0, **kw)
