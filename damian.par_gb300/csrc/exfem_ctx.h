@@ -259,6 +259,26 @@ int side_drm_next(Ctx &c, int par, F &&launch) {
 }
 int side_mark(Ctx &c);
 int side_join(Ctx &c);
+
+// Launches kernel k on the context's stream as a programmatic dependent of
+// the kernel before it (its blocks may start while that one drains and wait
+// in pdl_wait), unless exfem_opts.serial_launch is set or the launches are
+// being timed one by one.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dep(Ctx &c, void (*k)(KArgs...), unsigned grid, unsigned block, Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = c.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    const bool dep = c.opts.serial_launch == 0 && !c.prof_on;
+    cfg.attrs = dep ? attr : nullptr;
+    cfg.numAttrs = dep ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 // bf16 <-> float on the host (round to nearest even), for tests and read-back.
 float bf16_to_float(unsigned short h);
 

@@ -5,6 +5,16 @@
 
 #include "exfem_ctx.h"
 
+// Programmatic dependent launch (griddepcontrol): pdl_wait blocks the thread
+// until the grids this one depends on have completed and their writes are
+// visible (at once in a grid launched without the attribute); pdl_trigger
+// lets the next grid of the stream launch once every block of this one has
+// issued it or exited.  A kernel launched as a programmatic dependent touches
+// nothing an earlier kernel writes, and writes nothing an earlier kernel
+// reads, before its pdl_wait.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 namespace exfem {
 
 // Offset of (dof d, rhs r) within a node's 2R state values, or within a DRM

@@ -274,15 +274,6 @@ __device__ __forceinline__ unsigned short f2bf(float f) { return __bfloat16_as_u
 
 __device__ __forceinline__ int read_step(const DevModel &m) { return *(volatile int *)m.d_step; }
 
-// Programmatic dependent launch (griddepcontrol): pdl_wait blocks the thread
-// until the grids this one depends on have completed and their writes are
-// visible (at once in a grid launched without the attribute); pdl_trigger
-// lets the next grid of the stream launch once every block of this one has
-// issued it or exited.  A kernel launched as a programmatic dependent touches
-// nothing an earlier kernel writes, and writes nothing an earlier kernel
-// reads, before its pdl_wait.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // DRM forces (model.f90:745-800) of step `step` for the FP32 form: travel
 // times in FP64, the Ricker terms and the boundary/exterior split in FP32.
@@ -1926,26 +1917,6 @@ int f32_init(Ctx &c) {
     return EXFEM_OK;
 }
 
-// Launches kernel k on the context's stream as a programmatic dependent of
-// the kernel before it (its blocks may start while that one drains and wait
-// in pdl_wait), unless exfem_opts.serial_launch is set or the launches are
-// being timed one by one.
-template <typename... KArgs, typename... Args>
-static cudaError_t launch_dep(Ctx &c, void (*k)(KArgs...), unsigned grid, unsigned block, Args &&...args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = c.stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    const bool dep = c.opts.serial_launch == 0 && !c.prof_on;
-    cfg.attrs = dep ? attr : nullptr;
-    cfg.numAttrs = dep ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
-}
-
 // k_step32 with 32- or 64-bit indices as the context allows.
 template <int RPT, bool TC, bool PAIR, bool SLOT>
 static cudaError_t step32(Ctx &c, const DevModel &m, int nb, int T, const float *uh, float *uhn) {
@@ -2079,7 +2050,16 @@ int f32_launch_step(Ctx &c, int par) {
     mark(c, c.opts.variant == 4 ? "k_step32p" : "k_step32");
     }
     if (c.drm_side) {   // the side stream's next launch may overwrite the slot this step read
-        const int rc = side_mark(c);
+        int rc = side_mark(c);
+        // The next step's forces (queued on the side stream above) are
+        // waited for here, before this step's hanging pass, not just before
+        // the next step kernel: that kernel is a programmatic dependent of
+        // the hanging pass and follows it with no event wait in between, so
+        // its order after the forces rests on the hanging pass's ordinary
+        // launch.  (With the FP64 element kernel launched as a programmatic
+        // dependent directly after such an event wait, its step read wrong
+        // DRM forces: seismograms off by up to 94%.)
+        if (!rc) rc = side_join(c);
         if (rc) return rc;
     }
     if (c.p32_n > 0) {

@@ -519,10 +519,15 @@ def test_programmatic_dependent_launch_keeps_results(use_graph):
     touching the state.  Bit-identical to serial launches, with graph replay
     and without, with the DRM forces inline and on the second stream, in the
     slot and list forms and the persistent grid."""
-    m = workloads.build("canyon", scale=0.55, steps=70, save_every=2, waves=EIGHT_WAVES[:2])
-    for kw in (dict(), dict(drm_inline=1), dict(variant=5), dict(variant=4)):
-        a, ua = run32(m, use_graph=use_graph, serial_launch=1, **kw)
-        b, ub = run32(m, use_graph=use_graph, **kw)
-        assert np.array_equal(a, b), kw
-        for r in range(m.problem.nrhs):
-            assert np.array_equal(ua[r], ub[r]), (kw, r)
+    canyon = workloads.build("canyon", scale=0.55, steps=70, save_every=2, waves=EIGHT_WAVES[:2])
+    # a small mesh whose step is shorter than the next step's DRM pass on
+    # the second stream: the forces are still being computed when the hanging
+    # pass could start
+    rect = workloads.build("homogeneous_rectangle", steps=120, save_every=1)
+    for m, kws in ((canyon, (dict(), dict(drm_inline=1), dict(variant=5), dict(variant=4))), (rect, (dict(),))):
+        for kw in kws:
+            a, ua = run32(m, use_graph=use_graph, serial_launch=1, **kw)
+            b, ub = run32(m, use_graph=use_graph, **kw)
+            assert np.array_equal(a, b), kw
+            for r in range(m.problem.nrhs):
+                assert np.array_equal(ua[r], ub[r]), (kw, r)
