@@ -1948,10 +1948,11 @@ static int step32_pick(Ctx &c, const DevModel &m, int nb, int T, const float *uh
     const bool pair = m.lg == rpt;
     const bool tc = SLOT ? m.tcorn4 != nullptr : m.tcorn != nullptr;
     cudaError_t e = cudaSuccess;
-    if (!tc) {   // few RHS (f32_term_corners): corners from econn
+    if (!tc) {   // few RHS (f32_term_corners, f32_slot_corners): corners from econn
         // below 64 RHS the direct gather's state is always grouped by the
         // thread's RHS (f32_alloc), so these rows are always paired
-        static_assert(f32_term_corners(5) && f32_interleave(4), "econn corners only with grouped rows");
+        static_assert(f32_term_corners(63) && f32_slot_corners(63) && f32_interleave(63),
+                      "econn corners only below 64 RHS, with grouped rows");
         if (!pair) {
             c.err = "internal: few-RHS step on the plain layout";
             return EXFEM_E_STATE;
